@@ -1,0 +1,166 @@
+/*
+ * oz_gb300.h -- C ABI of the GB300 Ozaki-scheme DGEMM library (liboz_gb300.so).
+ *
+ * Plain C types only (ints, doubles, pointers, an opaque handle).  The drop-in
+ * C++ header include/oz_aie.h is written on top of these functions, and the
+ * Python package ozaie_gb300 binds them with ctypes.
+ *
+ * Reference interface replaced (atlarge-research/ozAIE):
+ *   oz_aie::ozAIE_setup            include/oz_aie.h:182-300  -> ozgb_setup
+ *   oz_aie::ozAIE_DGEMM            include/oz_aie.h:311-349  -> ozgb_dgemm
+ *   oz_aie::convert_paired_i64_to_double_matrix
+ *                                  include/oz_aie.h:92-150   -> ozgb_convert_paired_i64_to_double
+ *   oz_aie::cleanup_xrt            include/oz_aie.h:153-170  -> ozgb_release
+ *   process-global state b, d, buffers (include/oz_aie.h:31-58) -> ozgb_handle
+ *
+ * Every function returns an ozgb_status (0 = success).  No function falls back
+ * to the CPU: without a usable CUDA device the compute entry points return
+ * OZGB_ERR_NO_DEVICE.
+ */
+#ifndef OZ_GB300_H
+#define OZ_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ozgb_context *ozgb_handle;
+
+typedef enum {
+    OZGB_OK = 0,
+    OZGB_ERR_DIMS = 1,          /* bad dimensions; ozAIE_setup's status 1 (include/oz_aie.h:187-191) */
+    OZGB_ERR_NO_DEVICE = 2,     /* no usable CUDA device; takes the place of ozAIE_setup's 2 (missing env) */
+    OZGB_ERR_EXEC = 3,          /* a kernel failed to launch or run; ozAIE_DGEMM's 3 (include/oz_aie.h:337-340) */
+    OZGB_ERR_IMAGE = 4,         /* no kernel image for this GPU; takes the place of ozAIE_setup's 4 (build failed) */
+    OZGB_ERR_NOT_SETUP = 5,     /* ozgb_dgemm called before ozgb_setup */
+    OZGB_ERR_DIM_MISMATCH = 6,  /* ozgb_dgemm dims differ from the last setup (the reference overruns its buffers) */
+    OZGB_ERR_ARG = 7,           /* null pointer or invalid option value */
+    OZGB_ERR_ALLOC = 8,         /* device memory allocation failed */
+    OZGB_ERR_TIMEOUT = 9,       /* a device-side wait ran out of time; the kernel stopped early */
+    OZGB_ERR_UNSUPPORTED = 10   /* the requested slices/bins exceed the exact-accumulation limits */
+} ozgb_status;
+
+typedef enum { OZGB_MODE_ACCURATE = 0, OZGB_MODE_FAST = 1 } ozgb_mode; /* oz_aie::Mode, include/oz_aie.h:82 */
+
+typedef enum {
+    OZGB_PROFILE_GB300 = 0,     /* fast: b=7, s=8, triangular; accurate: b=7, s=8, full pair set; RN */
+    OZGB_PROFILE_REFERENCE = 1  /* the reference's (b, d) tables (include/oz_aie.h:60-80), triangular, RZ decode */
+} ozgb_profile;
+
+typedef enum {
+    OZGB_ROUND_DEFAULT = -1,     /* profile's choice */
+    OZGB_ROUND_NEAREST = 0,      /* exact bin sum rounded to nearest even, IEEE subnormals/overflow */
+    OZGB_ROUND_REFERENCE = 1     /* the reference's truncating decode (include/oz_aie.h:124-146) */
+} ozgb_rounding;
+
+/* Effective configuration of the last setup / call. */
+typedef struct {
+    int bits;        /* b: magnitude bits per slice */
+    int slices;      /* s (the reference's d / num_splits) */
+    int bins;        /* J: pair set {p + q <= J - 1}; J = s triangular, J = 2s - 1 full */
+    int rounding;    /* ozgb_rounding */
+    int tile_n;      /* BN of the slice-pair GEMM */
+    int k_chunk;     /* K elements per pipeline stage */
+    int stages;      /* pipeline stages */
+    int drain_chunks;/* K chunks accumulated in fp32 before a drain (exactness period) */
+    int acc_words;   /* 32-bit words of the exact per-element accumulator */
+    int pairs;       /* slice-pair products per K step */
+} ozgb_config;
+
+/* ---------------------------------------------------------------- handles */
+ozgb_status ozgb_create(ozgb_handle *out);
+ozgb_status ozgb_destroy(ozgb_handle h);
+/* Frees device buffers, keeps options; counterpart of cleanup_xrt (include/oz_aie.h:153-170). */
+ozgb_status ozgb_release(ozgb_handle h);
+
+/* ------------------------------------------------------------ drop-in path */
+/* ozAIE_setup (include/oz_aie.h:182): picks (b, s, J) for `mode` and sizes device
+ * buffers.  Accepts any M, N, K >= 1 (a superset of the reference's square
+ * power-of-two 128..2048). */
+ozgb_status ozgb_setup(ozgb_handle h, int M, int N, int K, int mode);
+/* ozAIE_DGEMM (include/oz_aie.h:311): C = A B on row-major host arrays
+ * (alpha = 1, beta = 0, C overwritten).  Dims must equal the last setup. */
+ozgb_status ozgb_dgemm(ozgb_handle h, int M, int N, int K, const double *A, const double *B, double *C);
+
+/* --------------------------------------------------------- device pointers */
+/* Same product on device arrays with leading dimensions, enqueued on `stream`
+ * (a cudaStream_t; NULL = the handle's stream).  Returns after enqueueing;
+ * ozgb_sync() reports device-side errors.  Uses the mode of the last setup
+ * (or OZGB_MODE_FAST when there was none). */
+ozgb_status ozgb_dgemm_device(ozgb_handle h, int M, int N, int K, const double *dA, long lda,
+                              const double *dB, long ldb, double *dC, long ldc, void *stream);
+/* Waits for the last enqueued call and checks the device error word. */
+ozgb_status ozgb_sync(ozgb_handle h);
+
+/* --------------------------------------------------------------- grouped */
+typedef struct {
+    int M, N, K;
+    const double *A; long lda; /* device pointers */
+    const double *B; long ldb;
+    double *C; long ldc;
+    double error_bound; /* requested normwise relative error; <= 0: use the handle's slices */
+    int slices_used;    /* out: slices chosen for this problem */
+} ozgb_problem;
+/* Many independent DGEMMs: one grouped launch per stage for all problems
+ * (optionally captured once into a CUDA graph and replayed, see
+ * ozgb_set_graph).  Enqueued on `stream`. */
+ozgb_status ozgb_dgemm_grouped(ozgb_handle h, ozgb_problem *probs, int n, void *stream);
+
+/* ---------------------------------------------------------------- options */
+ozgb_status ozgb_set_profile(ozgb_handle h, int profile);
+ozgb_status ozgb_set_bits(ozgb_handle h, int bits);        /* 0 = profile default */
+ozgb_status ozgb_set_slices(ozgb_handle h, int slices);    /* 0 = profile default */
+ozgb_status ozgb_set_bins(ozgb_handle h, int bins);        /* 0 = default, -1 = full pair set, else J */
+ozgb_status ozgb_set_rounding(ozgb_handle h, int rounding);
+/* Requested normwise relative error (> 0 enables slice selection from the
+ * exponent spread measured by stage (a)); 0 disables it. */
+ozgb_status ozgb_set_error_bound(ozgb_handle h, double bound);
+ozgb_status ozgb_set_graph(ozgb_handle h, int enable);     /* capture grouped launches in a CUDA graph */
+ozgb_status ozgb_set_timeout_ms(ozgb_handle h, double ms); /* device-side wait limit, default 2000 */
+ozgb_status ozgb_get_config(ozgb_handle h, ozgb_config *out);
+/* Per-stage device times of the last call (ms): [0] exponents, [1] split,
+ * [2] slice-pair GEMM + accumulation, [3] total.  Needs ozgb_set_profiling(h, 1). */
+ozgb_status ozgb_set_profiling(ozgb_handle h, int enable);
+ozgb_status ozgb_stage_times(ozgb_handle h, float *ms, int n);
+const char *ozgb_last_error(ozgb_handle h);
+
+/* -------------------------------------------------------- test / debug hooks */
+/* Intermediates of one DGEMM on host arrays, for parity checks:
+ *  er[M], ec[N]            max exponents (stage a), may be NULL
+ *  a_slices[s][M][K]       int8 slices of A (stage b), may be NULL
+ *  b_slices[s][K][N]       int8 slices of B, may be NULL
+ *  q[M][N][4]              exact per-element accumulator as 128-bit two's
+ *                          complement (4 little-endian 32-bit words), for bins
+ *                          [bin_lo, bin_hi] only (stage c); may be NULL
+ * Uses the handle's current options (setup dims need not match). */
+ozgb_status ozgb_dump(ozgb_handle h, int M, int N, int K, const double *A, const double *B, int32_t *er,
+                      int32_t *ec, int8_t *a_slices, int8_t *b_slices, int32_t *q, int bin_lo, int bin_hi);
+/* Runs a kernel whose only wait is on an mbarrier that nothing arrives on, with
+ * the given limit; returns OZGB_ERR_TIMEOUT when the bounded wait gave up and the
+ * device stayed usable (tests the timeout path without faulting the GPU). */
+ozgb_status ozgb_selftest_timeout(ozgb_handle h, double timeout_ms);
+
+/* Host helper kept from the reference: decodes the 2 x int64 per element wire
+ * format (include/oz_aie.h:92-150), C[row*(2N) + 2col] = low, +1 = high. */
+ozgb_status ozgb_convert_paired_i64_to_double(const int64_t *C, double *result, int M, int N, int K,
+                                              int num_splits, int bits_per_slice);
+
+/* Host-only planning query (no device needed): the kernel configuration the
+ * library would use for an M x N x K product with `bits`, `slices`, `bins`. */
+int ozgb_plan_query(int M, int N, int K, int bits, int slices, int bins, ozgb_config *out);
+/* Host-only precision knob (no device needed): the smallest slice count whose
+ * a-priori normwise error estimate is <= bound, from the stage-(a) statistics
+ * (row/column max exponents and sums of squares).  Returns -1 on bad input. */
+int ozgb_choose_slices(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N,
+                       int K, int bits, double bound, double *estimate);
+
+/* Library version string. */
+const char *ozgb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OZ_GB300_H */

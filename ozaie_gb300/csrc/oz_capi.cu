@@ -1,0 +1,637 @@
+// oz_capi.cu -- the C ABI (include/oz_gb300.h): handles, the drop-in
+// setup/DGEMM pair on host arrays, the device-pointer and grouped entry points,
+// options, dumps for parity tests.
+//
+// Reference interface replaced (atlarge-research/ozAIE include/oz_aie.h):
+//   ozAIE_setup :182-300, ozAIE_DGEMM :311-349, convert_paired_i64_to_double_matrix
+//   :92-150, cleanup_xrt :153-170.  No CPU fallback: every compute entry point
+//   needs a CUDA device and reports OZGB_ERR_NO_DEVICE otherwise.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <bit>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/oz_gb300.h"
+#include "oz_internal.h"
+#include "oz_plan.h"
+
+using namespace ozgb;
+
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    bool ensure(size_t bytes) {
+        if (bytes <= cap && p) return true;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        if (cudaMalloc(&p, std::max<size_t>(bytes, 256)) != cudaSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+            return false;
+        }
+        cap = std::max<size_t>(bytes, 256);
+        return true;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+}  // namespace
+
+struct ozgb_context {
+    std::mutex mu;
+    int device = -1;
+    bool setup_done = false;
+    int M = 0, N = 0, K = 0, mode = OZGB_MODE_FAST;
+    // options
+    int profile = OZGB_PROFILE_GB300;
+    int opt_bits = 0, opt_slices = 0, opt_bins = 0, opt_rounding = OZGB_ROUND_DEFAULT;
+    double err_bound = 0.0;
+    int use_graph = 0;
+    unsigned long long timeout_ns = 2000000000ull;
+    // last effective plan
+    Plan last{};
+    bool have_last = false;
+    // buffers
+    DevBuf a, b, c, at, bt, er, ec, ssr, ssc, err, raw;
+    cudaStream_t stream = nullptr;
+    // profiling
+    bool profiling = false;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool ev_recorded = false;
+    std::string msg;
+};
+
+namespace {
+
+ozgb_status fail(ozgb_handle h, ozgb_status st, const std::string &m) {
+    if (h) h->msg = m;
+    return st;
+}
+
+ozgb_status cuda_fail(ozgb_handle h, cudaError_t e, const char *what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorNoKernelImageForDevice || e == cudaErrorInvalidDeviceFunction) return fail(h, OZGB_ERR_IMAGE, m);
+    if (e == cudaErrorMemoryAllocation) return fail(h, OZGB_ERR_ALLOC, m);
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return fail(h, OZGB_ERR_NO_DEVICE, m);
+    return fail(h, OZGB_ERR_EXEC, m);
+}
+
+ozgb_status ensure_device(ozgb_handle h) {
+    if (h->device >= 0) {
+        cudaError_t e = cudaSetDevice(h->device);
+        return e == cudaSuccess ? OZGB_OK : cuda_fail(h, e, "cudaSetDevice");
+    }
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n < 1) {
+        cudaGetLastError();
+        return fail(h, OZGB_ERR_NO_DEVICE, "no CUDA device available (no CPU fallback)");
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return fail(h, OZGB_ERR_NO_DEVICE, "device query failed");
+    if (prop.major != 10 || prop.minor != 3)
+        return fail(h, OZGB_ERR_IMAGE, std::string("kernels are built for sm_103a; device is ") + prop.name);
+    if ((e = cudaSetDevice(dev)) != cudaSuccess) return cuda_fail(h, e, "cudaSetDevice");
+    if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return cuda_fail(h, e, "cudaStreamCreate");
+    for (auto &ev : h->ev)
+        if ((e = cudaEventCreate(&ev)) != cudaSuccess) return cuda_fail(h, e, "cudaEventCreate");
+    if (!h->err.ensure(sizeof(int))) return fail(h, OZGB_ERR_ALLOC, "device error word");
+    cudaMemset(h->err.p, 0, sizeof(int));
+    h->device = dev;
+    return OZGB_OK;
+}
+
+// Effective (b, s, J, rounding) for a call with inner dimension K.
+OzConfig resolve_config(ozgb_handle h, int K, int mode) {
+    OzConfig c;
+    if (h->profile == OZGB_PROFILE_REFERENCE) {
+        reference_table(K, mode, &c.b, &c.s);
+        c.J = c.s;
+        c.rounding = OUT_RZ_REF;
+    } else {
+        c.b = 7;
+        c.s = 8;
+        c.J = (mode == OZGB_MODE_FAST) ? c.s : 2 * c.s - 1;
+        c.rounding = OUT_RN;
+    }
+    if (h->opt_bits > 0) c.b = h->opt_bits;
+    if (h->opt_slices > 0) {
+        const bool full = (c.J == 2 * c.s - 1) && c.s > 1;
+        c.s = h->opt_slices;
+        c.J = full ? 2 * c.s - 1 : c.s;
+    }
+    if (h->opt_bins == -1) c.J = 2 * c.s - 1;
+    else if (h->opt_bins > 0) c.J = h->opt_bins;
+    if (h->opt_rounding >= 0) c.rounding = h->opt_rounding;
+    return c;
+}
+
+struct Operands {
+    int M, N, K;
+    const double *A;
+    long lda;
+    const double *B;
+    long ldb;
+    double *C;
+    long ldc;
+};
+
+// Stage (a): exponents (+ sums of squares when the precision knob needs them).
+ozgb_status enqueue_exponents(ozgb_handle h, const Operands &o, bool want_ss, cudaStream_t st) {
+    if (!h->er.ensure(sizeof(int32_t) * o.M) || !h->ec.ensure(sizeof(int32_t) * o.N))
+        return fail(h, OZGB_ERR_ALLOC, "exponent buffers");
+    double *ssr = nullptr, *ssc = nullptr;
+    if (want_ss) {
+        if (!h->ssr.ensure(sizeof(double) * o.M) || !h->ssc.ensure(sizeof(double) * o.N))
+            return fail(h, OZGB_ERR_ALLOC, "statistics buffers");
+        ssr = static_cast<double *>(h->ssr.p);
+        ssc = static_cast<double *>(h->ssc.p);
+        cudaMemsetAsync(ssc, 0, sizeof(double) * o.N, st);
+    }
+    cudaMemsetAsync(h->ec.p, 0, sizeof(int32_t) * o.N, st);
+    launch_rowmax(o.A, o.lda, o.M, o.K, static_cast<int32_t *>(h->er.p), ssr, st);
+    launch_colmax(o.B, o.ldb, o.K, o.N, static_cast<int32_t *>(h->ec.p), ssc, st);
+    return OZGB_OK;
+}
+
+ozgb_status choose_config(ozgb_handle h, const Operands &o, int mode, cudaStream_t st, OzConfig *cfg) {
+    *cfg = resolve_config(h, o.K, mode);
+    if (h->err_bound > 0.0 && h->opt_slices <= 0) {
+        // precision knob: needs the stage-(a) statistics on the host
+        std::vector<int32_t> er(o.M), ec(o.N);
+        std::vector<double> ssr(o.M), ssc(o.N);
+        cudaMemcpyAsync(er.data(), h->er.p, sizeof(int32_t) * o.M, cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(ec.data(), h->ec.p, sizeof(int32_t) * o.N, cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(ssr.data(), h->ssr.p, sizeof(double) * o.M, cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(ssc.data(), h->ssc.p, sizeof(double) * o.N, cudaMemcpyDeviceToHost, st);
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return cuda_fail(h, e, "statistics readback");
+        double est = 0;
+        const int s = choose_slices(er.data(), ssr.data(), o.M, ec.data(), ssc.data(), o.N, o.K, cfg->b,
+                                    h->err_bound, 2, 16, &est);
+        cfg->s = s;
+        cfg->J = s;
+    }
+    return OZGB_OK;
+}
+
+// Stages (b) and (c)+(d) for one problem whose exponents are in h->er / h->ec.
+ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, int out_mode, int bin_lo, int bin_hi,
+                               int32_t *raw, cudaStream_t st) {
+    if (!h->at.ensure(p.a_elems * 2) || !h->bt.ensure(p.b_elems * 2))
+        return fail(h, OZGB_ERR_ALLOC, "slice buffers");
+    uint16_t *at = static_cast<uint16_t *>(h->at.p), *bt = static_cast<uint16_t *>(h->bt.p);
+    launch_split_a(o.A, o.lda, o.M, o.K, static_cast<int32_t *>(h->er.p), p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.Mp, at, st);
+    launch_split_b(o.B, o.ldb, o.K, o.N, static_cast<int32_t *>(h->ec.p), p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.BN, p.Np,
+                   bt, st);
+    if (h->profiling) cudaEventRecord(h->ev[2], st);
+    GemmArgs g;
+    memset(&g, 0, sizeof g);
+    g.a_tiles = at;
+    g.b_tiles = bt;
+    g.er = static_cast<int32_t *>(h->er.p);
+    g.ec = static_cast<int32_t *>(h->ec.p);
+    g.c = o.C;
+    g.ldc = o.ldc;
+    g.raw = raw;
+    g.M = o.M;
+    g.N = o.N;
+    g.n_kc = p.n_kc;
+    g.KC = p.KC;
+    g.s = p.cfg.s;
+    g.J = p.cfg.J;
+    g.b = p.cfg.b;
+    g.KBc = p.KBc;
+    g.G = p.G;
+    g.bin_lo = bin_lo;
+    g.bin_hi = bin_hi;
+    g.out_mode = out_mode;
+    g.tiles_m = p.tiles_m;
+    g.tiles_n = p.tiles_n;
+    g.stages = p.stages;
+    g.stage_bytes = p.stage_bytes;
+    g.a_block_bytes = p.a_block_bytes;
+    g.b_block_bytes = p.b_block_bytes;
+    g.tmem_cols = p.tmem_cols;
+    g.err = static_cast<int *>(h->err.p);
+    g.timeout_ns = h->timeout_ns;
+    for (int i = 0; i < p.G; ++i) {
+        g.grp_lo[i] = p.grp_lo[i];
+        g.grp_hi[i] = p.grp_hi[i];
+    }
+    p.fn(g, p.tiles_m * p.tiles_n, p.smem, st);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(h, e, "slice-pair GEMM launch");
+    return OZGB_OK;
+}
+
+// The whole pipeline for one problem on device operands.
+ozgb_status enqueue_dgemm(ozgb_handle h, const Operands &o, int mode, cudaStream_t st, int out_mode_override = -1,
+                          int bin_lo = 0, int bin_hi = kMaxBins, int32_t *raw = nullptr) {
+    if (h->profiling) cudaEventRecord(h->ev[0], st);
+    const bool want_ss = h->err_bound > 0.0 && h->opt_slices <= 0;
+    ozgb_status rc = enqueue_exponents(h, o, want_ss, st);
+    if (rc) return rc;
+    if (h->profiling) cudaEventRecord(h->ev[1], st);
+    OzConfig cfg;
+    if ((rc = choose_config(h, o, mode, st, &cfg))) return rc;
+    Plan p;
+    std::string why;
+    if (!make_plan(o.M, o.N, o.K, cfg, &p, &why)) return fail(h, OZGB_ERR_UNSUPPORTED, why);
+    h->last = p;
+    h->have_last = true;
+    const int om = out_mode_override >= 0 ? out_mode_override : cfg.rounding;
+    if ((rc = enqueue_split_gemm(h, o, p, om, bin_lo, std::min(bin_hi, cfg.J - 1), raw, st))) return rc;
+    if (h->profiling) {
+        cudaEventRecord(h->ev[3], st);
+        h->ev_recorded = true;
+    }
+    return OZGB_OK;
+}
+
+ozgb_status check_device_error(ozgb_handle h, cudaStream_t st) {
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "kernel execution");
+    int word = 0;
+    e = cudaMemcpy(&word, h->err.p, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(h, e, "error word readback");
+    if (word != 0) {
+        cudaMemset(h->err.p, 0, sizeof(int));
+        return fail(h, OZGB_ERR_TIMEOUT,
+                    "a device-side wait ran out of time (code " + std::to_string(word) + "); the kernel stopped early");
+    }
+    return OZGB_OK;
+}
+
+bool valid_mode(int mode) { return mode == OZGB_MODE_ACCURATE || mode == OZGB_MODE_FAST; }
+
+}  // namespace
+
+extern "C" {
+
+const char *ozgb_version(void) { return "oz-gb300 0.1 (sm_103a, tcgen05 kind::f16 carrier)"; }
+
+ozgb_status ozgb_create(ozgb_handle *out) {
+    if (!out) return OZGB_ERR_ARG;
+    *out = new (std::nothrow) ozgb_context();
+    return *out ? OZGB_OK : OZGB_ERR_ALLOC;
+}
+
+ozgb_status ozgb_release(ozgb_handle h) {
+    if (!h) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (h->device >= 0) cudaSetDevice(h->device);
+    for (DevBuf *b : {&h->a, &h->b, &h->c, &h->at, &h->bt, &h->er, &h->ec, &h->ssr, &h->ssc, &h->raw}) b->release();
+    h->setup_done = false;
+    return OZGB_OK;
+}
+
+ozgb_status ozgb_destroy(ozgb_handle h) {
+    if (!h) return OZGB_ERR_ARG;
+    ozgb_release(h);
+    if (h->device >= 0) {
+        cudaSetDevice(h->device);
+        h->err.release();
+        for (auto &ev : h->ev)
+            if (ev) cudaEventDestroy(ev);
+        if (h->stream) cudaStreamDestroy(h->stream);
+    }
+    delete h;
+    return OZGB_OK;
+}
+
+ozgb_status ozgb_setup(ozgb_handle h, int M, int N, int K, int mode) {
+    if (!h) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (M < 1 || N < 1 || K < 1) return fail(h, OZGB_ERR_DIMS, "dimensions must be positive");
+    if (!valid_mode(mode)) return fail(h, OZGB_ERR_ARG, "mode must be accurate (0) or fast (1)");
+    ozgb_status rc = ensure_device(h);
+    if (rc) return rc;
+    OzConfig cfg = resolve_config(h, K, mode);
+    Plan p;
+    std::string why;
+    if (!make_plan(M, N, K, cfg, &p, &why)) return fail(h, OZGB_ERR_UNSUPPORTED, why);
+    const size_t nA = static_cast<size_t>(M) * K, nB = static_cast<size_t>(K) * N, nC = static_cast<size_t>(M) * N;
+    if (!h->a.ensure(nA * 8) || !h->b.ensure(nB * 8) || !h->c.ensure(nC * 8) || !h->at.ensure(p.a_elems * 2) ||
+        !h->bt.ensure(p.b_elems * 2) || !h->er.ensure(4 * M) || !h->ec.ensure(4 * N))
+        return fail(h, OZGB_ERR_ALLOC, "device buffers for the setup shape");
+    h->M = M;
+    h->N = N;
+    h->K = K;
+    h->mode = mode;
+    h->setup_done = true;
+    h->last = p;
+    h->have_last = true;
+    return OZGB_OK;
+}
+
+ozgb_status ozgb_dgemm(ozgb_handle h, int M, int N, int K, const double *A, const double *B, double *C) {
+    if (!h) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (!h->setup_done) return fail(h, OZGB_ERR_NOT_SETUP, "ozgb_setup must be called first");
+    if (M != h->M || N != h->N || K != h->K)
+        return fail(h, OZGB_ERR_DIM_MISMATCH, "dimensions differ from the last setup");
+    if (!A || !B || !C) return fail(h, OZGB_ERR_ARG, "null matrix pointer");
+    ozgb_status rc = ensure_device(h);
+    if (rc) return rc;
+    const size_t nA = static_cast<size_t>(M) * K, nB = static_cast<size_t>(K) * N, nC = static_cast<size_t>(M) * N;
+    if (!h->a.ensure(nA * 8) || !h->b.ensure(nB * 8) || !h->c.ensure(nC * 8))
+        return fail(h, OZGB_ERR_ALLOC, "operand buffers");
+    cudaStream_t st = h->stream;
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(h->a.p, A, nA * 8, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return cuda_fail(h, e, "copy A");
+    if ((e = cudaMemcpyAsync(h->b.p, B, nB * 8, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return cuda_fail(h, e, "copy B");
+    Operands o{M, N, K, static_cast<double *>(h->a.p), K, static_cast<double *>(h->b.p), N,
+               static_cast<double *>(h->c.p), N};
+    if ((rc = enqueue_dgemm(h, o, h->mode, st))) {
+        cudaStreamSynchronize(st);
+        return rc;
+    }
+    if ((e = cudaMemcpyAsync(C, h->c.p, nC * 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return cuda_fail(h, e, "copy C");
+    return check_device_error(h, st);
+}
+
+ozgb_status ozgb_dgemm_device(ozgb_handle h, int M, int N, int K, const double *dA, long lda, const double *dB,
+                              long ldb, double *dC, long ldc, void *stream) {
+    if (!h) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (M < 1 || N < 1 || K < 1) return fail(h, OZGB_ERR_DIMS, "dimensions must be positive");
+    if (!dA || !dB || !dC) return fail(h, OZGB_ERR_ARG, "null matrix pointer");
+    if (lda < K || ldb < N || ldc < N) return fail(h, OZGB_ERR_ARG, "leading dimension too small");
+    ozgb_status rc = ensure_device(h);
+    if (rc) return rc;
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : h->stream;
+    Operands o{M, N, K, dA, lda, dB, ldb, dC, ldc};
+    return enqueue_dgemm(h, o, h->setup_done ? h->mode : OZGB_MODE_FAST, st);
+}
+
+ozgb_status ozgb_sync(ozgb_handle h) {
+    if (!h) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (h->device < 0) return fail(h, OZGB_ERR_NO_DEVICE, "no call was made on a device");
+    cudaSetDevice(h->device);
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_fail(h, e, "device synchronize");
+    return check_device_error(h, h->stream);
+}
+
+ozgb_status ozgb_dgemm_grouped(ozgb_handle h, ozgb_problem *probs, int n, void *stream) {
+    if (!h || (!probs && n > 0) || n < 0) return OZGB_ERR_ARG;
+    // First version: the problems run one after another on the stream (a fused
+    // grouped launch replaces this loop).
+    for (int i = 0; i < n; ++i) {
+        ozgb_problem &pb = probs[i];
+        double saved = h->err_bound;
+        if (pb.error_bound > 0) h->err_bound = pb.error_bound;
+        ozgb_status rc =
+            ozgb_dgemm_device(h, pb.M, pb.N, pb.K, pb.A, pb.lda, pb.B, pb.ldb, pb.C, pb.ldc, stream);
+        h->err_bound = saved;
+        if (rc) return rc;
+        pb.slices_used = h->last.cfg.s;
+    }
+    return OZGB_OK;
+}
+
+ozgb_status ozgb_set_profile(ozgb_handle h, int profile) {
+    if (!h || (profile != OZGB_PROFILE_GB300 && profile != OZGB_PROFILE_REFERENCE)) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->profile = profile;
+    return OZGB_OK;
+}
+ozgb_status ozgb_set_bits(ozgb_handle h, int bits) {
+    if (!h || bits < 0 || bits > 7) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->opt_bits = bits;
+    return OZGB_OK;
+}
+ozgb_status ozgb_set_slices(ozgb_handle h, int slices) {
+    if (!h || slices < 0 || slices > 40) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->opt_slices = slices;
+    return OZGB_OK;
+}
+ozgb_status ozgb_set_bins(ozgb_handle h, int bins) {
+    if (!h || bins < -1 || bins > kMaxBins) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->opt_bins = bins;
+    return OZGB_OK;
+}
+ozgb_status ozgb_set_rounding(ozgb_handle h, int rounding) {
+    if (!h || rounding < -1 || rounding > 1) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->opt_rounding = rounding;
+    return OZGB_OK;
+}
+ozgb_status ozgb_set_error_bound(ozgb_handle h, double bound) {
+    if (!h || !(bound >= 0.0)) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->err_bound = bound;
+    return OZGB_OK;
+}
+ozgb_status ozgb_set_graph(ozgb_handle h, int enable) {
+    if (!h) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->use_graph = enable ? 1 : 0;
+    return OZGB_OK;
+}
+ozgb_status ozgb_set_timeout_ms(ozgb_handle h, double ms) {
+    if (!h || !(ms > 0.0)) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->timeout_ns = static_cast<unsigned long long>(ms * 1e6);
+    return OZGB_OK;
+}
+ozgb_status ozgb_set_profiling(ozgb_handle h, int enable) {
+    if (!h) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->profiling = enable != 0;
+    h->ev_recorded = false;
+    return OZGB_OK;
+}
+
+ozgb_status ozgb_stage_times(ozgb_handle h, float *ms, int n) {
+    if (!h || !ms || n < 1) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (!h->ev_recorded) return fail(h, OZGB_ERR_ARG, "no profiled call recorded");
+    cudaEventSynchronize(h->ev[3]);
+    float t[4] = {0, 0, 0, 0};
+    cudaEventElapsedTime(&t[0], h->ev[0], h->ev[1]);
+    cudaEventElapsedTime(&t[1], h->ev[1], h->ev[2]);
+    cudaEventElapsedTime(&t[2], h->ev[2], h->ev[3]);
+    cudaEventElapsedTime(&t[3], h->ev[0], h->ev[3]);
+    for (int i = 0; i < n && i < 4; ++i) ms[i] = t[i];
+    return OZGB_OK;
+}
+
+ozgb_status ozgb_get_config(ozgb_handle h, ozgb_config *out) {
+    if (!h || !out) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (!h->have_last) return fail(h, OZGB_ERR_NOT_SETUP, "no setup or call yet");
+    const Plan &p = h->last;
+    out->bits = p.cfg.b;
+    out->slices = p.cfg.s;
+    out->bins = p.cfg.J;
+    out->rounding = p.cfg.rounding;
+    out->tile_n = p.BN;
+    out->k_chunk = p.KC;
+    out->stages = p.stages;
+    out->drain_chunks = p.KBc;
+    out->acc_words = p.W;
+    out->pairs = p.pairs;
+    return OZGB_OK;
+}
+
+const char *ozgb_last_error(ozgb_handle h) { return h ? h->msg.c_str() : "null handle"; }
+
+ozgb_status ozgb_dump(ozgb_handle h, int M, int N, int K, const double *A, const double *B, int32_t *er, int32_t *ec,
+                      int8_t *a_slices, int8_t *b_slices, int32_t *q, int bin_lo, int bin_hi) {
+    if (!h || !A || !B) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (M < 1 || N < 1 || K < 1) return fail(h, OZGB_ERR_DIMS, "dimensions must be positive");
+    ozgb_status rc = ensure_device(h);
+    if (rc) return rc;
+    cudaStream_t st = h->stream;
+    const size_t nA = static_cast<size_t>(M) * K, nB = static_cast<size_t>(K) * N, nC = static_cast<size_t>(M) * N;
+    if (!h->a.ensure(nA * 8) || !h->b.ensure(nB * 8) || !h->c.ensure(nC * 8) || !h->raw.ensure(nC * 16))
+        return fail(h, OZGB_ERR_ALLOC, "dump buffers");
+    cudaMemcpyAsync(h->a.p, A, nA * 8, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(h->b.p, B, nB * 8, cudaMemcpyHostToDevice, st);
+    Operands o{M, N, K, static_cast<double *>(h->a.p), K, static_cast<double *>(h->b.p), N,
+               static_cast<double *>(h->c.p), N};
+    if ((rc = enqueue_dgemm(h, o, h->setup_done ? h->mode : OZGB_MODE_FAST, st, OUT_RAW, bin_lo, bin_hi,
+                            static_cast<int32_t *>(h->raw.p))))
+        return rc;
+    if ((rc = check_device_error(h, st))) return rc;
+    const Plan &p = h->last;
+    if (er) cudaMemcpy(er, h->er.p, 4 * M, cudaMemcpyDeviceToHost);
+    if (ec) cudaMemcpy(ec, h->ec.p, 4 * N, cudaMemcpyDeviceToHost);
+    if (q) cudaMemcpy(q, h->raw.p, nC * 16, cudaMemcpyDeviceToHost);
+    const int s = p.cfg.s;
+    auto bf16_to_int = [](uint16_t v) {
+        uint32_t u = static_cast<uint32_t>(v) << 16;
+        float f;
+        memcpy(&f, &u, 4);
+        return static_cast<int8_t>(f);
+    };
+    if (a_slices) {
+        std::vector<uint16_t> t(p.a_elems);
+        cudaMemcpy(t.data(), h->at.p, p.a_elems * 2, cudaMemcpyDeviceToHost);
+        for (int sl = 0; sl < s; ++sl)
+            for (int m = 0; m < M; ++m)
+                for (int k = 0; k < K; ++k) {
+                    const size_t off = ((static_cast<size_t>(m >> 7) * p.n_kc + k / p.KC) * s + sl) * BM * p.KC +
+                                       canon_offset(m & 127, k % p.KC, p.KC);
+                    a_slices[(static_cast<size_t>(sl) * M + m) * K + k] = bf16_to_int(t[off]);
+                }
+    }
+    if (b_slices) {
+        std::vector<uint16_t> t(p.b_elems);
+        cudaMemcpy(t.data(), h->bt.p, p.b_elems * 2, cudaMemcpyDeviceToHost);
+        for (int sl = 0; sl < s; ++sl)
+            for (int k = 0; k < K; ++k)
+                for (int n = 0; n < N; ++n) {
+                    const size_t off = ((static_cast<size_t>(n / p.BN) * p.n_kc + k / p.KC) * s + sl) *
+                                           static_cast<size_t>(p.BN) * p.KC +
+                                       canon_offset(n % p.BN, k % p.KC, p.KC);
+                    b_slices[(static_cast<size_t>(sl) * K + k) * N + n] = bf16_to_int(t[off]);
+                }
+    }
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? OZGB_OK : cuda_fail(h, e, "dump readback");
+}
+
+ozgb_status ozgb_selftest_timeout(ozgb_handle h, double timeout_ms) {
+    if (!h || !(timeout_ms > 0.0)) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    ozgb_status rc = ensure_device(h);
+    if (rc) return rc;
+    launch_selftest_timeout(static_cast<int *>(h->err.p), static_cast<unsigned long long>(timeout_ms * 1e6),
+                            h->stream);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(h, e, "selftest launch");
+    return check_device_error(h, h->stream);
+}
+
+// include/oz_aie.h:92-150 restated on the host: int128 = lo + sext51(hi) << (g0 b),
+// truncated to 53 bits, exponent from the embedded Er+Ec.
+ozgb_status ozgb_convert_paired_i64_to_double(const int64_t *C, double *result, int M, int N, int K, int num_splits,
+                                              int bits_per_slice) {
+    if (!C || !result || M < 0 || N < 0 || K < 1 || num_splits < 1 || bits_per_slice < 1) return OZGB_ERR_ARG;
+    const int b = bits_per_slice, d = num_splits;
+    const int alignable = 31 / b + 1;
+    const int numer = b * (d + 1) - 51 + std::countr_zero(static_cast<unsigned>(K));
+    const int minfirst = numer < 0 ? 1 : numer / b + 1;
+    const int g0 = std::min(d, std::max(minfirst, alignable));
+    for (long i = 0; i < static_cast<long>(M) * N; ++i) {
+        const int64_t lo = C[2 * i], hi = C[2 * i + 1];
+        const uint64_t escale = (static_cast<uint64_t>(hi) >> 51) & 0xFFFu;
+        uint64_t hm = static_cast<uint64_t>(hi) & 0x0007FFFFFFFFFFFFull;
+        if (hi < 0) hm |= 0xFFF8000000000000ull;
+        __int128 quad = static_cast<__int128>(lo) + (static_cast<__int128>(static_cast<int64_t>(hm)) << (g0 * b));
+        const bool neg = quad < 0;
+        unsigned __int128 mag = neg ? static_cast<unsigned __int128>(-quad) : static_cast<unsigned __int128>(quad);
+        const uint64_t mh = static_cast<uint64_t>(mag >> 64), ml = static_cast<uint64_t>(mag);
+        const int L = mh ? 128 - std::countl_zero(mh) : (ml ? 64 - std::countl_zero(ml) : 0);
+        const long long exponent = static_cast<long long>(L) - b * (d + 1) - 1;
+        const int shift = L - 53;
+        uint64_t lu = shift > 0 ? static_cast<uint64_t>(mag >> shift) : static_cast<uint64_t>(mag << -shift);
+        if (lu > 0) {
+            lu -= 0x0010000000000000ull;
+            lu += (neg ? 0x8000000000000000ull : 0ull) + (static_cast<uint64_t>(exponent + 1023) << 52) +
+                  (static_cast<uint64_t>(static_cast<long long>(escale) + 2 - 2046) << 52);
+        }
+        memcpy(&result[i], &lu, 8);
+    }
+    return OZGB_OK;
+}
+
+// Host-only planning queries (no device needed): used by tests and tools.
+int ozgb_plan_query(int M, int N, int K, int bits, int slices, int bins, ozgb_config *out) {
+    OzConfig c;
+    c.b = bits;
+    c.s = slices;
+    c.J = bins;
+    Plan p;
+    std::string why;
+    if (!make_plan(M, N, K, c, &p, &why)) return OZGB_ERR_UNSUPPORTED;
+    if (out) {
+        out->bits = p.cfg.b;
+        out->slices = p.cfg.s;
+        out->bins = p.cfg.J;
+        out->rounding = p.cfg.rounding;
+        out->tile_n = p.BN;
+        out->k_chunk = p.KC;
+        out->stages = p.stages;
+        out->drain_chunks = p.KBc;
+        out->acc_words = p.W;
+        out->pairs = p.pairs;
+    }
+    return OZGB_OK;
+}
+
+int ozgb_choose_slices(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N, int K,
+                       int bits, double bound, double *estimate) {
+    if (!er || !ssr || !ec || !ssc || M < 1 || N < 1 || K < 1 || bits < 1 || !(bound > 0)) return -1;
+    return choose_slices(er, ssr, M, ec, ssc, N, K, bits, bound, 2, 16, estimate);
+}
+
+}  // extern "C"

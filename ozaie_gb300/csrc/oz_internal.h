@@ -1,0 +1,85 @@
+// oz_internal.h -- shared definitions of the GB300 Ozaki DGEMM kernels and host code.
+//
+// Data layout in HBM (written by stage (b), read by stage (c)):
+//   A slices: for each 128-row tile mt and K chunk c, the s slices of that block
+//     are one contiguous region  [mt][c][p][128 rows x KC]  of bf16, and
+//   B slices (of B^T, i.e. N rows with K contiguous):  [nt][c][q][BN rows x KC].
+//   Inside a (rows x KC) block the elements follow the tcgen05 K-major canonical
+//   layout without swizzle: 8-row x 8-element (16-byte) core matrices, the core
+//   matrices of an 8-row group consecutive along K (LBO = 128 B), 8-row groups
+//   KC*16 bytes apart (SBO).  One bulk copy moves a whole stage.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#if defined(__CUDACC__)
+#define OZ_HD __host__ __device__
+#else
+#define OZ_HD
+#endif
+
+namespace ozgb {
+
+constexpr int BM = 128;         // rows of A per tile (UMMA M)
+constexpr int kMaxBins = 64;      // J limit
+constexpr int kMaxGroups = 64;    // drain groups limit
+constexpr int kThreads = 320;     // warp 0 producer, warp 1 MMA issuer, warps 2..9 drain + epilogue
+constexpr int kEpiWarps = 8;
+constexpr int kMaxAccWords = 5;
+
+enum OutMode : int { OUT_RN = 0, OUT_RZ_REF = 1, OUT_RAW = 2 };
+
+// Element offset of (row r, k) inside one (rows x KC) canonical block.
+OZ_HD inline long canon_offset(int r, int kk, int KC) {
+    return (long)(((r >> 3) * (KC >> 3) + (kk >> 3)) * 64 + (r & 7) * 8 + (kk & 7));
+}
+
+struct GemmArgs {
+    const uint16_t *a_tiles;
+    const uint16_t *b_tiles;
+    const int32_t *er;
+    const int32_t *ec;
+    double *c;
+    long ldc;
+    int32_t *raw;  // OUT_RAW: [M][N][4] words
+    int M, N;
+    int n_kc, KC, s, J, b;
+    int KBc, G;
+    int bin_lo, bin_hi;
+    int out_mode;
+    int tiles_m, tiles_n;
+    int stages;
+    uint32_t stage_bytes, a_block_bytes, b_block_bytes;
+    uint32_t tmem_cols;
+    int *err;
+    unsigned long long timeout_ns;
+    int grp_lo[kMaxGroups], grp_hi[kMaxGroups];
+};
+
+// Device error codes written to the error word.
+enum DevErr : int { DEVERR_NONE = 0, DEVERR_TIMEOUT_PRODUCER = 1, DEVERR_TIMEOUT_MMA = 2, DEVERR_TIMEOUT_EPI = 3,
+                    DEVERR_TIMEOUT_SELFTEST = 4 };
+
+typedef void (*GemmLaunchFn)(const GemmArgs &args, int grid, size_t smem, void *stream);
+
+// Kernel variants (tile N x accumulator words); defined in oz_gemm_bn*.cu.
+void launch_gemm_128_2(const GemmArgs &, int, size_t, void *);
+void launch_gemm_64_3(const GemmArgs &, int, size_t, void *);
+void launch_gemm_64_4(const GemmArgs &, int, size_t, void *);
+void launch_gemm_48_3(const GemmArgs &, int, size_t, void *);
+void launch_gemm_48_4(const GemmArgs &, int, size_t, void *);
+void launch_gemm_32_4(const GemmArgs &, int, size_t, void *);
+void launch_gemm_32_5(const GemmArgs &, int, size_t, void *);
+void launch_gemm_16_4(const GemmArgs &, int, size_t, void *);
+void launch_gemm_16_5(const GemmArgs &, int, size_t, void *);
+
+// Stage (a) / (b) launches (oz_split.cu).
+void launch_rowmax(const double *A, long lda, int M, int K, int32_t *er, double *ss, void *stream);
+void launch_colmax(const double *B, long ldb, int K, int N, int32_t *ec, double *ss, void *stream);
+void launch_split_a(const double *A, long lda, int M, int K, const int32_t *er, int b, int s, int KC, int n_kc,
+                    int Mp, uint16_t *tiles, void *stream);
+void launch_split_b(const double *B, long ldb, int K, int N, const int32_t *ec, int b, int s, int KC, int n_kc,
+                    int BN, int Np, uint16_t *tiles, void *stream);
+int launch_selftest_timeout(int *err, unsigned long long timeout_ns, void *stream);
+
+}  // namespace ozgb

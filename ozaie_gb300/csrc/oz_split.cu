@@ -1,0 +1,230 @@
+// oz_split.cu -- stages (a) and (b): per-row / per-column maximum exponent and the
+// error-free split of FP64 values into signed b-bit slices.
+//
+// Reference semantics (atlarge-research/ozAIE, src/aie_kernels/generic/ozaki_base.cc):
+//   (a) ozaki_get_max_exponent_inner_tiled_wise_half_half  :342-440  (max of bits 52..62, start 0)
+//   (b) extract_splits_acc64_half_half                     :449-639  (see split_value below)
+// All work on the FP64 bit patterns is integer; FP64 arithmetic appears only in
+// the optional sum of squares that the precision knob reads.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "oz_internal.h"
+#include "oz_ptx.cuh"
+
+namespace ozgb {
+
+__device__ __forceinline__ int exp_field(double x) {
+    return static_cast<int>((static_cast<unsigned long long>(__double_as_longlong(x)) >> 52) & 0x7FF);
+}
+
+// ------------------------------------------------------------- stage (a)
+// One warp per row of A: max exponent field (and sum of squares when ss != null).
+__global__ void k_rowmax(const double *__restrict__ A, long lda, int M, int K, int32_t *__restrict__ er,
+                         double *__restrict__ ss) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= M) return;
+    const double *row = A + static_cast<size_t>(warp) * lda;
+    int e = 0;
+    double s2 = 0.0;
+    for (int k = lane; k < K; k += 32) {
+        const double x = __ldg(row + k);
+        e = max(e, exp_field(x));
+        if (ss) s2 = fma(x, x, s2);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+        if (ss) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    if (lane == 0) {
+        er[warp] = e;
+        if (ss) ss[warp] = s2;
+    }
+}
+
+// One thread per column of B over a slab of rows; combined with atomicMax
+// (ec must be zeroed first) and, when ss != null, atomicAdd of squares.
+__global__ void k_colmax(const double *__restrict__ B, long ldb, int K, int N, int rows_per_slab,
+                         int32_t *__restrict__ ec, double *__restrict__ ss) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    const int k0 = blockIdx.y * rows_per_slab;
+    const int k1 = min(K, k0 + rows_per_slab);
+    int e = 0;
+    double s2 = 0.0;
+    for (int k = k0; k < k1; ++k) {
+        const double x = __ldg(B + static_cast<size_t>(k) * ldb + n);
+        e = max(e, exp_field(x));
+        if (ss) s2 = fma(x, x, s2);
+    }
+    atomicMax(ec + n, e);
+    if (ss) atomicAdd(ss + n, s2);
+}
+
+// ------------------------------------------------------------- stage (b)
+// The reference's split of one double (ozaki_base.cc:497-628), restated:
+//   bias = E - e (uint32), mantissa with implicit one for normal numbers only,
+//   m64 = mant << 11 (MSB at bit 63), words w0..w3 selected by bias >= 32/64/96
+//   (w3 not cleared for bias >= 128 when two 64-bit windows are used),
+//   X = (w0:w1:w2:w3) >> (bias mod 32),
+//   slice_i = sign * ((X >> (128 - b(i+1))) & (2^b - 1)).
+struct SplitState {
+    unsigned __int128 X;
+    bool neg;
+};
+
+__device__ __forceinline__ SplitState split_value(double x, int E, bool two_windows) {
+    const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(x));
+    const uint32_t e = static_cast<uint32_t>((u >> 52) & 0x7FF);
+    const unsigned long long mant = (u & ((1ull << 52) - 1)) | (e ? (1ull << 52) : 0ull);
+    const uint32_t bias = static_cast<uint32_t>(E) - e;
+    const unsigned long long m64 = mant << 11;
+    const uint32_t vhi = static_cast<uint32_t>(m64 >> 32), vlo = static_cast<uint32_t>(m64);
+    const uint32_t w0 = bias >= 32u ? 0u : vhi;
+    const uint32_t w1 = bias >= 64u ? 0u : (bias >= 32u ? vhi : vlo);
+    uint32_t w2 = 0, w3 = 0;
+    if (two_windows) {
+        w2 = bias >= 96u ? 0u : (bias >= 64u ? vhi : (bias >= 32u ? vlo : 0u));
+        w3 = bias >= 96u ? vhi : (bias >= 64u ? vlo : 0u);
+    }
+    const unsigned __int128 W = (static_cast<unsigned __int128>((static_cast<unsigned long long>(w0) << 32) | w1)
+                                 << 64) |
+                                static_cast<unsigned __int128>((static_cast<unsigned long long>(w2) << 32) | w3);
+    SplitState st;
+    st.X = W >> (bias & 31u);
+    st.neg = (u >> 63) != 0;
+    return st;
+}
+
+__device__ __forceinline__ uint32_t slice_bf16(const SplitState &st, int i, int b) {
+    const int sh = 128 - b * (i + 1);
+    int v = sh >= 0 ? static_cast<int>(static_cast<uint32_t>(st.X >> sh) & ((1u << b) - 1u)) : 0;
+    if (st.neg) v = -v;
+    // |v| <= 127 is exact in bf16: the top half of the fp32 pattern
+    return __float_as_uint(static_cast<float>(v)) >> 16;
+}
+
+__host__ __device__ inline bool split_two_windows(int b, int s) {
+    const int avoid = 1 + (b == 3 ? 3 : 0);
+    const int nv0 = 64 - avoid - ((64 - avoid) % b);
+    return s * b > nv0;
+}
+
+// A [M][K] row-major -> A slice blocks [mt][c][p][128 x KC].  One thread takes 8
+// consecutive K values of one row and writes one 16-byte piece per slice; a warp
+// covers 8 rows x 32 K (4 core matrices of each slice, 512 contiguous bytes).
+__global__ void k_split_a(const double *__restrict__ A, long lda, int M, int K, const int32_t *__restrict__ er,
+                          int b, int s, int KC, int n_kc, int Mp, uint16_t *__restrict__ tiles) {
+    const int r8 = threadIdx.x & 7;
+    const int kgl = threadIdx.x >> 3;  // 0..31
+    const int m = blockIdx.y * 8 + r8;
+    const int k0 = (blockIdx.x * 32 + kgl) * 8;
+    const int Kp = n_kc * KC;
+    if (m >= Mp || k0 >= Kp) return;
+    const bool two = split_two_windows(b, s);
+    const int E = m < M ? er[m] : 0;
+    SplitState st[8];
+    const double *row = A + static_cast<size_t>(m) * lda;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int k = k0 + i;
+        const double x = (m < M && k < K) ? __ldg(row + k) : 0.0;
+        st[i] = split_value(x, E, two);
+    }
+    const int mt = m >> 7, r = m & 127, c = k0 / KC, kk = k0 % KC;
+    const size_t slice_elems = static_cast<size_t>(BM) * KC;
+    uint16_t *dst = tiles + (static_cast<size_t>(mt) * n_kc + c) * s * slice_elems + canon_offset(r, kk, KC);
+    for (int p = 0; p < s; ++p) {
+        uint4 v;
+        v.x = slice_bf16(st[0], p, b) | (slice_bf16(st[1], p, b) << 16);
+        v.y = slice_bf16(st[2], p, b) | (slice_bf16(st[3], p, b) << 16);
+        v.z = slice_bf16(st[4], p, b) | (slice_bf16(st[5], p, b) << 16);
+        v.w = slice_bf16(st[6], p, b) | (slice_bf16(st[7], p, b) << 16);
+        *reinterpret_cast<uint4 *>(dst + p * slice_elems) = v;
+    }
+}
+
+// B [K][N] row-major -> slice blocks of B^T [nt][c][q][BN x KC].  One thread
+// takes one column n and 8 consecutive K; a warp reads 32 consecutive columns
+// per row (coalesced) and writes four 128-byte core matrices per slice.
+__global__ void k_split_b(const double *__restrict__ B, long ldb, int K, int N, const int32_t *__restrict__ ec,
+                          int b, int s, int KC, int n_kc, int BN, int Np, uint16_t *__restrict__ tiles) {
+    const int n = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int k0 = (blockIdx.y * 8 + (threadIdx.x >> 5)) * 8;
+    const int Kp = n_kc * KC;
+    if (n >= Np || k0 >= Kp) return;
+    const bool two = split_two_windows(b, s);
+    const int E = n < N ? ec[n] : 0;
+    SplitState st[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int k = k0 + i;
+        const double x = (n < N && k < K) ? __ldg(B + static_cast<size_t>(k) * ldb + n) : 0.0;
+        st[i] = split_value(x, E, two);
+    }
+    const int nt = n / BN, r = n % BN, c = k0 / KC, kk = k0 % KC;
+    const size_t slice_elems = static_cast<size_t>(BN) * KC;
+    uint16_t *dst = tiles + (static_cast<size_t>(nt) * n_kc + c) * s * slice_elems + canon_offset(r, kk, KC);
+    for (int q = 0; q < s; ++q) {
+        uint4 v;
+        v.x = slice_bf16(st[0], q, b) | (slice_bf16(st[1], q, b) << 16);
+        v.y = slice_bf16(st[2], q, b) | (slice_bf16(st[3], q, b) << 16);
+        v.z = slice_bf16(st[4], q, b) | (slice_bf16(st[5], q, b) << 16);
+        v.w = slice_bf16(st[6], q, b) | (slice_bf16(st[7], q, b) << 16);
+        *reinterpret_cast<uint4 *>(dst + q * slice_elems) = v;
+    }
+}
+
+// A kernel whose only wait is on an mbarrier that nothing arrives on: exercises
+// the bounded-wait path (records DEVERR_TIMEOUT_SELFTEST and returns).
+__global__ void k_selftest_timeout(int *err, unsigned long long timeout_ns) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int zero = 0;
+        if (!mbar_wait(&bar, 0, &zero, timeout_ns)) atomicCAS(err, 0, DEVERR_TIMEOUT_SELFTEST);
+    }
+}
+
+// ---------------------------------------------------------------- launches
+void launch_rowmax(const double *A, long lda, int M, int K, int32_t *er, double *ss, void *stream) {
+    const int threads = 256;
+    const int blocks = (M * 32 + threads - 1) / threads;
+    k_rowmax<<<blocks, threads, 0, static_cast<cudaStream_t>(stream)>>>(A, lda, M, K, er, ss);
+}
+
+void launch_colmax(const double *B, long ldb, int K, int N, int32_t *ec, double *ss, void *stream) {
+    const int threads = 256;
+    const int rows = 64;
+    dim3 grid((N + threads - 1) / threads, (K + rows - 1) / rows);
+    k_colmax<<<grid, threads, 0, static_cast<cudaStream_t>(stream)>>>(B, ldb, K, N, rows, ec, ss);
+}
+
+void launch_split_a(const double *A, long lda, int M, int K, const int32_t *er, int b, int s, int KC, int n_kc,
+                    int Mp, uint16_t *tiles, void *stream) {
+    const int Kp = n_kc * KC;
+    dim3 grid((Kp / 8 + 31) / 32, Mp / 8);
+    k_split_a<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(A, lda, M, K, er, b, s, KC, n_kc, Mp, tiles);
+}
+
+void launch_split_b(const double *B, long ldb, int K, int N, const int32_t *ec, int b, int s, int KC, int n_kc,
+                    int BN, int Np, uint16_t *tiles, void *stream) {
+    const int Kp = n_kc * KC;
+    dim3 grid((Np + 31) / 32, (Kp / 8 + 7) / 8);
+    k_split_b<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(B, ldb, K, N, ec, b, s, KC, n_kc, BN, Np,
+                                                                    tiles);
+}
+
+int launch_selftest_timeout(int *err, unsigned long long timeout_ns, void *stream) {
+    k_selftest_timeout<<<1, 32, 0, static_cast<cudaStream_t>(stream)>>>(err, timeout_ns);
+    return 0;
+}
+
+}  // namespace ozgb
