@@ -68,6 +68,10 @@ typedef struct {
     int drain_chunks;/* K chunks accumulated in fp32 before a drain (exactness period) */
     int acc_words;   /* 32-bit words of the exact per-element accumulator */
     int pairs;       /* slice-pair products per K step */
+    int blocks;      /* bin blocks (one UMMA accumulator range each) */
+    int umma_per_kstep; /* UMMAs per 16-deep K step */
+    int block_lo[8]; /* first bin of each block */
+    int block_nb[8]; /* bins in each block */
 } ozgb_config;
 
 /* ---------------------------------------------------------------- handles */
@@ -87,7 +91,7 @@ ozgb_status ozgb_dgemm(ozgb_handle h, int M, int N, int K, const double *A, cons
 
 /* --------------------------------------------------------- device pointers */
 /* Same product on device arrays with leading dimensions, enqueued on `stream`
- * (a cudaStream_t; NULL = the handle's stream).  Returns after enqueueing;
+ * (a cudaStream_t; NULL = the CUDA default stream).  Returns after enqueueing;
  * ozgb_sync() reports device-side errors.  Uses the mode of the last setup
  * (or OZGB_MODE_FAST when there was none). */
 ozgb_status ozgb_dgemm_device(ozgb_handle h, int M, int N, int K, const double *dA, long lda,

@@ -24,10 +24,18 @@ class OzgbConfig(ctypes.Structure):
         ("drain_chunks", ctypes.c_int),
         ("acc_words", ctypes.c_int),
         ("pairs", ctypes.c_int),
+        ("blocks", ctypes.c_int),
+        ("umma_per_kstep", ctypes.c_int),
+        ("block_lo", ctypes.c_int * 8),
+        ("block_nb", ctypes.c_int * 8),
     ]
 
     def as_dict(self):
-        return {f: getattr(self, f) for f, _ in self._fields_}
+        d = {}
+        for f, _ in self._fields_:
+            v = getattr(self, f)
+            d[f] = list(v)[: self.blocks] if f in ("block_lo", "block_nb") else v
+        return d
 
 
 class OzgbProblem(ctypes.Structure):
@@ -84,7 +92,9 @@ SIGNATURES = [
 
 
 def lib_path():
-    return _build.LIB
+    """liboz_gb300.so in the package directory, or the path in OZGB_LIB_PATH
+    (an alternative build of the same library, e.g. one with cycle probes)."""
+    return os.environ.get("OZGB_LIB_PATH") or _build.LIB
 
 
 def load(build_if_missing=True):

@@ -18,7 +18,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/oz_gb300.h"
+#include "oz_gb300.h"
 #include "oz_internal.h"
 #include "oz_plan.h"
 
@@ -67,7 +67,8 @@ struct ozgb_context {
     bool have_last = false;
     // buffers
     DevBuf a, b, c, at, bt, er, ec, ssr, ssc, err, raw;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;       // used by the host-array entry points
+    cudaStream_t last_stream = nullptr;  // stream of the last enqueued call
     // profiling
     bool profiling = false;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -193,8 +194,8 @@ ozgb_status choose_config(ozgb_handle h, const Operands &o, int mode, cudaStream
 }
 
 // Stages (b) and (c)+(d) for one problem whose exponents are in h->er / h->ec.
-ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, int out_mode, int bin_lo, int bin_hi,
-                               int32_t *raw, cudaStream_t st) {
+ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, int out_mode, int32_t *raw,
+                               cudaStream_t st) {
     if (!h->at.ensure(p.a_elems * 2) || !h->bt.ensure(p.b_elems * 2))
         return fail(h, OZGB_ERR_ALLOC, "slice buffers");
     uint16_t *at = static_cast<uint16_t *>(h->at.p), *bt = static_cast<uint16_t *>(h->bt.p);
@@ -218,10 +219,6 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
     g.s = p.cfg.s;
     g.J = p.cfg.J;
     g.b = p.cfg.b;
-    g.KBc = p.KBc;
-    g.G = p.G;
-    g.bin_lo = bin_lo;
-    g.bin_hi = bin_hi;
     g.out_mode = out_mode;
     g.tiles_m = p.tiles_m;
     g.tiles_n = p.tiles_n;
@@ -229,22 +226,59 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
     g.stage_bytes = p.stage_bytes;
     g.a_block_bytes = p.a_block_bytes;
     g.b_block_bytes = p.b_block_bytes;
+    g.b_pad_lo_bytes = static_cast<uint32_t>(p.pad_lo) * p.b_slice_bytes;
+    g.b_region_bytes = p.b_region_bytes;
     g.tmem_cols = p.tmem_cols;
     g.err = static_cast<int *>(h->err.p);
     g.timeout_ns = h->timeout_ns;
+    g.G = p.G;
     for (int i = 0; i < p.G; ++i) {
-        g.grp_lo[i] = p.grp_lo[i];
-        g.grp_hi[i] = p.grp_hi[i];
+        g.blk_lo[i] = p.blk_lo[i];
+        g.blk_nb[i] = p.blk_nb[i];
+        g.blk_p0[i] = p.blk_p0[i];
+        g.blk_p1[i] = p.blk_p1[i];
+        g.blk_period[i] = p.blk_period[i];
+        g.blk_off[i] = p.blk_off[i];
     }
+#ifdef OZGB_PROBE
+    // probe builds: per-CTA cycle counters of the GEMM roles, summarised on stderr
+    static unsigned long long *probe = nullptr;
+    static size_t probe_n = 0;
+    const size_t need = static_cast<size_t>(p.tiles_m) * p.tiles_n * 8;
+    if (probe_n < need) {
+        if (probe) cudaFree(probe);
+        cudaMalloc(&probe, need * 8);
+        probe_n = need;
+    }
+    cudaMemsetAsync(probe, 0, need * 8, st);
+    g.probe = probe;
+#endif
     p.fn(g, p.tiles_m * p.tiles_n, p.smem, st);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(h, e, "slice-pair GEMM launch");
+#ifdef OZGB_PROBE
+    {
+        cudaStreamSynchronize(st);
+        std::vector<unsigned long long> hp(need);
+        cudaMemcpy(hp.data(), probe, need * 8, cudaMemcpyDeviceToHost);
+        double sum[8] = {0};
+        for (size_t i = 0; i < need; ++i) sum[i % 8] += static_cast<double>(hp[i]);
+        const double n = static_cast<double>(need / 8);
+        fprintf(stderr,
+                "OZGB_PROBE ctas=%.0f avg cycles per CTA: producer_wait=%.0f mma_wait_full=%.0f "
+                "mma_wait_drained=%.0f mma_issue=%.0f drain_wait=%.0f drain_work=%.0f epilogue=%.0f total=%.0f "
+                "(n_kc=%d blocks=%d)\n",
+                n, sum[0] / n, sum[1] / n, sum[2] / n, sum[3] / n, sum[4] / n, sum[5] / n, sum[6] / n, sum[7] / n,
+                p.n_kc, p.G);
+    }
+#endif
     return OZGB_OK;
 }
 
 // The whole pipeline for one problem on device operands.
 ozgb_status enqueue_dgemm(ozgb_handle h, const Operands &o, int mode, cudaStream_t st, int out_mode_override = -1,
                           int bin_lo = 0, int bin_hi = kMaxBins, int32_t *raw = nullptr) {
+    h->last_stream = st;
     if (h->profiling) cudaEventRecord(h->ev[0], st);
     const bool want_ss = h->err_bound > 0.0 && h->opt_slices <= 0;
     ozgb_status rc = enqueue_exponents(h, o, want_ss, st);
@@ -254,11 +288,11 @@ ozgb_status enqueue_dgemm(ozgb_handle h, const Operands &o, int mode, cudaStream
     if ((rc = choose_config(h, o, mode, st, &cfg))) return rc;
     Plan p;
     std::string why;
-    if (!make_plan(o.M, o.N, o.K, cfg, &p, &why)) return fail(h, OZGB_ERR_UNSUPPORTED, why);
+    if (!make_plan(o.M, o.N, o.K, cfg, &p, &why, bin_lo, bin_hi)) return fail(h, OZGB_ERR_UNSUPPORTED, why);
     h->last = p;
     h->have_last = true;
     const int om = out_mode_override >= 0 ? out_mode_override : cfg.rounding;
-    if ((rc = enqueue_split_gemm(h, o, p, om, bin_lo, std::min(bin_hi, cfg.J - 1), raw, st))) return rc;
+    if ((rc = enqueue_split_gemm(h, o, p, om, raw, st))) return rc;
     if (h->profiling) {
         cudaEventRecord(h->ev[3], st);
         h->ev_recorded = true;
@@ -281,6 +315,15 @@ ozgb_status check_device_error(ozgb_handle h, cudaStream_t st) {
 }
 
 bool valid_mode(int mode) { return mode == OZGB_MODE_ACCURATE || mode == OZGB_MODE_FAST; }
+
+void fill_blocks(const Plan &p, ozgb_config *out) {
+    out->blocks = p.G;
+    out->umma_per_kstep = p.mma_per_kstep;
+    for (int i = 0; i < 8; ++i) {
+        out->block_lo[i] = i < p.G ? p.blk_lo[i] : 0;
+        out->block_nb[i] = i < p.G ? p.blk_nb[i] : 0;
+    }
+}
 
 }  // namespace
 
@@ -380,7 +423,7 @@ ozgb_status ozgb_dgemm_device(ozgb_handle h, int M, int N, int K, const double *
     if (lda < K || ldb < N || ldc < N) return fail(h, OZGB_ERR_ARG, "leading dimension too small");
     ozgb_status rc = ensure_device(h);
     if (rc) return rc;
-    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : h->stream;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL: the default (legacy) stream
     Operands o{M, N, K, dA, lda, dB, ldb, dC, ldc};
     return enqueue_dgemm(h, o, h->setup_done ? h->mode : OZGB_MODE_FAST, st);
 }
@@ -392,7 +435,7 @@ ozgb_status ozgb_sync(ozgb_handle h) {
     cudaSetDevice(h->device);
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return cuda_fail(h, e, "device synchronize");
-    return check_device_error(h, h->stream);
+    return check_device_error(h, h->last_stream);
 }
 
 ozgb_status ozgb_dgemm_grouped(ozgb_handle h, ozgb_problem *probs, int n, void *stream) {
@@ -494,9 +537,10 @@ ozgb_status ozgb_get_config(ozgb_handle h, ozgb_config *out) {
     out->tile_n = p.BN;
     out->k_chunk = p.KC;
     out->stages = p.stages;
-    out->drain_chunks = p.KBc;
+    out->drain_chunks = p.min_period;
     out->acc_words = p.W;
     out->pairs = p.pairs;
+    fill_blocks(p, out);
     return OZGB_OK;
 }
 
@@ -621,9 +665,10 @@ int ozgb_plan_query(int M, int N, int K, int bits, int slices, int bins, ozgb_co
         out->tile_n = p.BN;
         out->k_chunk = p.KC;
         out->stages = p.stages;
-        out->drain_chunks = p.KBc;
+        out->drain_chunks = p.min_period;
         out->acc_words = p.W;
         out->pairs = p.pairs;
+    fill_blocks(p, out);
     }
     return OZGB_OK;
 }

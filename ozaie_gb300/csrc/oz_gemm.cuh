@@ -11,20 +11,26 @@
 //   * Carrier: tcgen05.mma kind::f16 with bf16 slices (|v| <= 127 is exact in
 //     bf16) and fp32 accumulators in TMEM.  (kind::i8 is not accepted by ptxas
 //     for sm_103a.)  Every partial sum is an integer of magnitude <= 2^24 as
-//     long as a bin accumulates at most KB = KBc*KC K-values between drains,
-//     pairs_in_bin * KB * (2^b-1)^2 <= 2^24, so the fp32 accumulation is exact.
+//     long as bin j accumulates at most KB_j K-values between drains,
+//     pairs_in_bin(j) * KB_j * (2^b-1)^2 <= 2^24, so the fp32 accumulation is exact.
 //   * TMEM holds one fp32 accumulator of BN columns per bin j (column j*BN).
-//     All pairs (p, q) of a bin group that share A_p are one MMA: the B slices
-//     q = j-p for consecutive bins j are consecutive in shared memory and the
-//     bins are consecutive in TMEM, so A_p is read once per group, not per pair.
-//   * Bins are split into G contiguous groups; group g is drained after chunks
-//     c with (c+1) % KBc == g.  The MMA issuer walks the groups of a chunk in
-//     the rotation (c+1+t) % KBc, so the group that drains after this chunk is
-//     issued first and the group drained after the previous chunk is issued
-//     last: the drain of one group overlaps the MMAs of all the others.
+//     Bins are partitioned into up to 8 blocks of at most 256 columns.  Every
+//     UMMA of a block spans the whole block: A slice p against the B slices
+//     q = j - p of all bins j of the block, which are consecutive in shared
+//     memory; q outside [0, s) reads zero slices padded below and above the
+//     loaded ones.  On GB300 one M=128, K=16 UMMA costs max(~114, N/2) cycles
+//     and a UMMA into an accumulator range that partly overlaps the previous
+//     one costs more, so full-block UMMAs (large N, identical ranges) beat
+//     per-pair ones despite the padded zero work.  The planner picks the
+//     partition with a dynamic program over that cost.
+//   * Each block is a drain group with its own period (its tightest bin).  In
+//     each chunk the MMA issuer first issues the blocks that drain after this
+//     chunk, then the others, and last the blocks drained after the previous
+//     chunk (after waiting for their drain): a drain overlaps the UMMAs of the
+//     other blocks.  The first UMMA of a block after a drain overwrites the
+//     accumulators (enable_input_d = 0), so TMEM is never cleared explicitly.
 //   * Drain (warps 2..9): TMEM -> registers, fp32 -> int32 (exact), shifted by
-//     b(J-1-j) and added into a W-word two's complement accumulator per
-//     element; the columns are then zeroed for the next period.
+//     b(J-1-j) and added into a W-word two's complement accumulator per element.
 //   * Epilogue: the exact accumulator q is rounded once to FP64 with the scale
 //     2^{Er+Ec-2044-b(J+1)} (round-to-nearest, or the reference's truncating
 //     decode, or written raw for parity dumps).
@@ -42,8 +48,6 @@ namespace ozgb {
 // q += lo * 2^(32*K0) + hi * 2^(32*(K0+1)) + ext * (2^(32*(K0+2)) + ...), one carry chain.
 template <int W, int K0>
 struct QAdd;
-
-#define OZ_QADD_BODY_1(a) "add.u32 %" #a ", %" #a ", %W0;\n\t"
 
 template <>
 struct QAdd<2, 0> {
@@ -254,13 +258,44 @@ __device__ __forceinline__ double q_to_double(const uint32_t (&q)[W], int escale
     return __longlong_as_double(static_cast<long long>(bits));
 }
 
+// ------------------------------------------------------------ drain schedule
+// Block g is drained after chunk c when (c + 1 + blk_off[g]) % blk_period[g] == 0,
+// and every block after the last chunk.  The MMA issuer and the drain warps step
+// identical copies of this schedule.
+struct DrainSchedule {
+    int r[kMaxGroups];
+    __device__ __forceinline__ void init(const GemmArgs &g) {
+#pragma unroll
+        for (int i = 0; i < kMaxGroups; ++i) r[i] = (i < g.G) ? (1 + g.blk_off[i]) % g.blk_period[i] : 1;
+    }
+    // Mask of the blocks drained after the current chunk; advances to the next chunk.
+    __device__ __forceinline__ uint32_t next(const GemmArgs &g, bool last) {
+        uint32_t m = 0;
+#pragma unroll
+        for (int i = 0; i < kMaxGroups; ++i) {
+            if (i < g.G) {
+                if (r[i] == 0) m |= 1u << i;
+                r[i] = (r[i] + 1 == g.blk_period[i]) ? 0 : r[i] + 1;
+            }
+        }
+        return last ? ((1u << g.G) - 1u) : m;
+    }
+};
+
+// Optional cycle probes (OZGB_PROBE builds only).
+#ifdef OZGB_PROBE
+#define OZ_PT(name) long long name = clock64()
+#define OZ_PADD(acc, t0) (acc) += clock64() - (t0)
+#else
+#define OZ_PT(name)
+#define OZ_PADD(acc, t0)
+#endif
+
 // ------------------------------------------------------------------ kernel
-template <int BN, int W>
+template <int BN, int W, int KC>
 __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_constant__ GemmArgs g) {
-    constexpr int HALF = BN / 2;        // columns per drain thread
-    constexpr int NLD = HALF / 8;       // 8-column TMEM loads per bin
-    constexpr int MAXB = 256 / BN;      // bins per MMA (N <= 256)
-    constexpr int DB = (HALF % 16 == 0) ? 16 : 8;  // columns per drain batch
+    constexpr int HALF = BN / 2;                  // columns per drain thread
+    constexpr int DB = (HALF <= 24) ? HALF : 16;  // columns per TMEM load batch
     static_assert(HALF % 8 == 0, "BN must be a multiple of 16");
 
     extern __shared__ uint8_t smem_raw[];
@@ -268,14 +303,26 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + static_cast<size_t>(g.stages) * g.stage_bytes);
     uint64_t *empty = full + g.stages;
     uint64_t *gfull = empty + g.stages;
-    uint64_t *gempty = gfull + g.G;
-    uint64_t *tmem_ready = gempty + g.G;
-    uint64_t *mma_done = tmem_ready + 1;
+    uint64_t *gempty = gfull + kMaxGroups;
+    uint64_t *mma_done = gempty + kMaxGroups;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mma_done + 1);
     int *abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
     volatile int *vabort = abort_flag;
+    // drain mask of the chunk held by each stage (written by the producer before it
+    // arms the stage), and the per-block UMMA parameters of the issuer
+    uint32_t *stage_mask = reinterpret_cast<uint32_t *>(abort_flag + 1);  // [stages <= 8]
+    uint64_t *blk_ad = reinterpret_cast<uint64_t *>(
+        (reinterpret_cast<uintptr_t>(stage_mask + 8) + 7) & ~uintptr_t(7));  // [kMaxGroups]
+    uint64_t *blk_bd = blk_ad + kMaxGroups;
+    uint32_t *blk_tm = reinterpret_cast<uint32_t *>(blk_bd + kMaxGroups);   // TMEM address
+    uint32_t *blk_id = blk_tm + kMaxGroups;                                 // instruction descriptor
+    int *blk_np = reinterpret_cast<int *>(blk_id + kMaxGroups);             // A slices per UMMA run
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#ifdef OZGB_PROBE
+    long long pr0 = 0, pr1 = 0, pr2 = 0, pr3 = 0;
+    const long long pstart = clock64();
+#endif
 
     // grouped rasterisation: 8 M-tiles share the same stream of B tiles
     int mt, nt;
@@ -291,6 +338,19 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
         nt = r / gm;
     }
 
+    // zero B slices below and above the loaded ones (read by out-of-range pairs)
+    {
+        const uint32_t pad_hi_bytes = g.b_region_bytes - g.b_pad_lo_bytes - g.b_block_bytes;
+        for (int st = 0; st < g.stages; ++st) {
+            uint8_t *breg = smem + static_cast<size_t>(st) * g.stage_bytes + g.a_block_bytes;
+            for (uint32_t i = threadIdx.x * 16; i < g.b_pad_lo_bytes; i += kThreads * 16)
+                *reinterpret_cast<uint4 *>(breg + i) = make_uint4(0, 0, 0, 0);
+            uint8_t *top = breg + g.b_pad_lo_bytes + g.b_block_bytes;
+            for (uint32_t i = threadIdx.x * 16; i < pad_hi_bytes; i += kThreads * 16)
+                *reinterpret_cast<uint4 *>(top + i) = make_uint4(0, 0, 0, 0);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
     if (threadIdx.x == 0) {
         for (int i = 0; i < g.stages; ++i) {
             mbar_init(&full[i], 1);
@@ -300,7 +360,6 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
             mbar_init(&gfull[i], 1);
             mbar_init(&gempty[i], kEpiWarps);
         }
-        mbar_init(tmem_ready, kEpiWarps);
         mbar_init(mma_done, 1);
         *abort_flag = (*reinterpret_cast<volatile int *>(g.err) != 0) ? 1 : 0;
         fence_mbar_init();
@@ -323,10 +382,16 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
             const uint8_t *b_src = reinterpret_cast<const uint8_t *>(g.b_tiles) +
                                    static_cast<size_t>(nt) * g.n_kc * g.b_block_bytes;
             int issued = 0;
+            int st = 0;
+            uint32_t eparity = 0;
+            DrainSchedule pds;
+            pds.init(g);
             for (int c = 0; c < g.n_kc; ++c) {
                 if (*vabort) break;
-                const int st = c % g.stages, round = c / g.stages;
-                if (round > 0 && !mbar_wait(&empty[st], (round - 1) & 1, vabort, TO)) {
+                OZ_PT(tw);
+                const bool got = (c < g.stages) || mbar_wait(&empty[st], eparity, vabort, TO);
+                OZ_PADD(pr0, tw);
+                if (!got) {
                     if (!*vabort) {
                         atomicCAS(g.err, 0, DEVERR_TIMEOUT_PRODUCER);
                         *vabort = 1;
@@ -334,11 +399,18 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                     break;
                 }
                 uint8_t *dst = smem + static_cast<size_t>(st) * g.stage_bytes;
+                stage_mask[st] = pds.next(g, c == g.n_kc - 1);  // published by the arrive below
                 mbar_arrive_expect_tx(&full[st], g.a_block_bytes + g.b_block_bytes);
                 bulk_g2s(dst, a_src + static_cast<size_t>(c) * g.a_block_bytes, g.a_block_bytes, &full[st]);
-                bulk_g2s(dst + g.a_block_bytes, b_src + static_cast<size_t>(c) * g.b_block_bytes, g.b_block_bytes,
-                         &full[st]);
+                bulk_g2s(dst + g.a_block_bytes + g.b_pad_lo_bytes, b_src + static_cast<size_t>(c) * g.b_block_bytes,
+                         g.b_block_bytes, &full[st]);
                 ++issued;
+                if (++st == g.stages) {
+                    st = 0;
+                    // the wait before reusing stage st in round r (>= 1) is on the
+                    // (r-1)-th completion of empty[st]: parity (r - 1) & 1
+                    if (c + 1 > g.stages) eparity ^= 1u;
+                }
             }
             // every copy issued must land before the CTA may exit
             const int zero = 0;
@@ -348,50 +420,96 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
     } else if (warp == 1) {
         // ---------------------------------------------------- MMA issuer
         if (lane == 0) {
-            bool ok = mbar_wait(tmem_ready, 0, vabort, TO);
-            tc_fence_after();
-            uint64_t ephase = 0;  // per-group parity of gempty waits
-            const uint32_t idesc_base = idesc_bf16_f32(BM, 16) & ~(0x3Fu << 17);
-            const uint32_t a_slice_bytes = BM * g.KC * 2;
-            const uint32_t b_slice_bytes = BN * g.KC * 2;
-            const uint32_t sbo = g.KC * 16;
-            for (int c = 0; ok && c < g.n_kc; ++c) {
-                const int st = c % g.stages, round = c / g.stages;
-                if (!mbar_wait(&full[st], round & 1, vabort, TO)) { ok = false; break; }
-                tc_fence_after();
-                const uint32_t a_base = smem_u32(smem + static_cast<size_t>(st) * g.stage_bytes);
-                const uint32_t b_base = a_base + g.a_block_bytes;
-                const bool last = (c == g.n_kc - 1);
-                for (int t = 0; t < g.KBc; ++t) {
-                    const int grp = (c + 1 + t) % g.KBc;
-                    if (grp >= g.G) continue;
-                    if (c >= 1 && grp == c % g.KBc) {
-                        if (!mbar_wait(&gempty[grp], static_cast<uint32_t>((ephase >> grp) & 1ull), vabort, TO)) {
-                            ok = false;
-                            break;
-                        }
-                        ephase ^= (1ull << grp);
-                        tc_fence_after();
+            constexpr uint32_t a_step = (BM * KC * 2) >> 4;  // descriptor units (16 B)
+            constexpr uint32_t b_step = (BN * KC * 2) >> 4;
+            constexpr uint32_t sbo = KC * 16;
+            constexpr int ksteps = KC >> 4;
+            {
+                // per-block UMMA parameters, once: with a single issuing thread every
+                // scalar instruction between UMMAs leaves the tensor core idle
+                const uint32_t a0 = smem_u32(smem);
+                const uint64_t ad0 = smem_desc(a0, 128, sbo);
+                const uint64_t bd0 = smem_desc(a0 + g.a_block_bytes + g.b_pad_lo_bytes, 128, sbo);
+                const uint32_t idesc_base = idesc_bf16_f32(BM, 16) & ~(0x3Fu << 17);
+#pragma unroll
+                for (int i = 0; i < kMaxGroups; ++i) {
+                    if (i < g.G) {
+                        blk_ad[i] = ad0 + static_cast<uint64_t>(g.blk_p0[i]) * a_step;
+                        blk_bd[i] = bd0 + static_cast<uint64_t>(static_cast<int64_t>(g.blk_lo[i] - g.blk_p0[i]) * b_step);
+                        blk_tm[i] = tmem + static_cast<uint32_t>(g.blk_lo[i] * BN);
+                        blk_id[i] = idesc_base | (static_cast<uint32_t>((g.blk_nb[i] * BN) >> 3) << 17);
+                        blk_np[i] = g.blk_p1[i] - g.blk_p0[i] + 1;
                     }
-                    const int glo = max(g.grp_lo[grp], g.bin_lo), ghi = min(g.grp_hi[grp], g.bin_hi);
-                    for (int kk = 0; kk < (g.KC >> 4); ++kk) {
-                        for (int p = 0; p < g.s; ++p) {
-                            const int jlo = max(glo, p), jhi = min(ghi, p + g.s - 1);
-                            for (int j0 = jlo; j0 <= jhi; j0 += MAXB) {
-                                const int j1 = min(jhi, j0 + MAXB - 1);
-                                const int n = (j1 - j0 + 1) * BN;
-                                const uint64_t ad = smem_desc(a_base + p * a_slice_bytes + kk * 256, 128, sbo);
-                                const uint64_t bd =
-                                    smem_desc(b_base + (j0 - p) * b_slice_bytes + kk * 256, 128, sbo);
-                                umma_bf16(tmem + static_cast<uint32_t>(j0 * BN), ad, bd,
-                                          idesc_base | (static_cast<uint32_t>(n >> 3) << 17), 1u);
-                            }
-                        }
-                    }
-                    if (((c + 1) % g.KBc) == grp || last) umma_commit(&gfull[grp]);
                 }
+            }
+            const uint32_t all = (1u << g.G) - 1u;
+            uint64_t ephase = 0;            // per-block parity of gempty waits
+            uint32_t prev = 0;              // blocks drained after the previous chunk
+            uint32_t fresh = all;           // blocks whose next UMMA overwrites the accumulators
+            int st = 0;
+            uint32_t fparity = 0;
+            bool ok = true;
+            for (int c = 0; ok && c < g.n_kc; ++c) {
+                OZ_PT(tf);
+                const bool gotf = mbar_wait(&full[st], fparity, vabort, TO);
+                OZ_PADD(pr0, tf);
+                if (!gotf) { ok = false; break; }
+                tc_fence_after();
+                OZ_PT(ti);
+                const uint64_t stage_off = (static_cast<uint64_t>(st) * g.stage_bytes) >> 4;
+                const uint32_t cur = stage_mask[st];
+                // issue order: blocks drained after this chunk, then the rest, then the
+                // blocks whose drain (after the previous chunk) must finish first
+                uint32_t order[3] = {cur & ~prev, all & ~cur & ~prev, prev};
+                for (int cls = 0; ok && cls < 3; ++cls) {
+                    uint32_t m = order[cls];
+                    while (m) {
+                        const int blk = __ffs(m) - 1;
+                        const uint32_t bit = 1u << blk;
+                        m &= m - 1;
+                        if (cls == 2) {
+                            OZ_PT(te);
+                            const bool gote = mbar_wait(&gempty[blk], static_cast<uint32_t>((ephase >> blk) & 1ull),
+                                                        vabort, TO);
+                            OZ_PADD(pr1, te);
+                            if (!gote) {
+                                ok = false;
+                                break;
+                            }
+                            ephase ^= (1ull << blk);
+                            tc_fence_after();
+                        }
+                        const uint32_t d_tmem = blk_tm[blk];
+                        const uint32_t idesc = blk_id[blk];
+                        const int np = blk_np[blk];
+                        uint64_t ad = blk_ad[blk] + stage_off;
+                        uint64_t bd = blk_bd[blk] + stage_off;
+                        uint32_t acc = (fresh & bit) ? 0u : 1u;
+                        for (int p = 0; p < np; ++p) {
+#pragma unroll
+                            for (int kk = 0; kk < ksteps; ++kk) {
+                                umma_bf16(d_tmem, ad + static_cast<uint64_t>(kk * 16), bd + static_cast<uint64_t>(kk * 16),
+                                          idesc, acc);
+                                acc = 1u;
+                            }
+                            ad += a_step;
+                            bd -= b_step;
+                        }
+                        fresh &= ~bit;
+                        if (cur & bit) {
+                            umma_commit(&gfull[blk]);
+                            fresh |= bit;
+                        }
+                    }
+                }
+                OZ_PADD(pr2, ti);
                 if (!ok) break;
                 umma_commit(&empty[st]);
+                if (++st == g.stages) {
+                    st = 0;
+                    fparity ^= 1u;
+                }
+                prev = cur;
             }
             if (!ok && !*vabort) {
                 atomicCAS(g.err, 0, DEVERR_TIMEOUT_MMA);
@@ -410,59 +528,65 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
         const int half = ew >> 2;
         const uint32_t trow = tmem + (static_cast<uint32_t>(32 * qd) << 16) + static_cast<uint32_t>(half * HALF);
 
-        for (int j = 0; j < g.J; ++j)
-#pragma unroll
-            for (int l = 0; l < NLD; ++l) tmem_st8_zero(trow + j * BN + l * 8);
-        tmem_st_wait();
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(tmem_ready);
-
         uint32_t q[HALF][W];
 #pragma unroll
         for (int i = 0; i < HALF; ++i)
 #pragma unroll
             for (int w = 0; w < W; ++w) q[i][w] = 0;
 
+        DrainSchedule ds;
+        ds.init(g);
         uint64_t fphase = 0;
+        uint32_t prev = 0;
         bool ok = true;
         for (int c = 0; ok && c < g.n_kc; ++c) {
             const bool last = (c == g.n_kc - 1);
-            const int ngr = last ? g.KBc : 1;
-            for (int t = 0; t < ngr; ++t) {
-                const int grp = (c + 1 + t) % g.KBc;
-                if (grp >= g.G) continue;
-                if (!mbar_wait(&gfull[grp], static_cast<uint32_t>((fphase >> grp) & 1ull), vabort, TO)) {
-                    ok = false;
-                    break;
-                }
-                fphase ^= (1ull << grp);
-                tc_fence_after();
-                const int glo = max(g.grp_lo[grp], g.bin_lo), ghi = min(g.grp_hi[grp], g.bin_hi);
-                for (int j = glo; j <= ghi; ++j) {
-                    const int sh = g.b * (g.J - 1 - j);
-#pragma unroll
-                    for (int cb = 0; cb < HALF / DB; ++cb) {
-                        uint32_t v[DB];
-#pragma unroll
-                        for (int l = 0; l < DB / 8; ++l) tmem_ld8(trow + j * BN + cb * DB + l * 8, v + l * 8);
-                        tmem_ld_wait();
-#pragma unroll
-                        for (int i = 0; i < DB; ++i) reg_fence(v[i]);
-                        if (!last) {
-#pragma unroll
-                            for (int l = 0; l < DB / 8; ++l) tmem_st8_zero(trow + j * BN + cb * DB + l * 8);
-                        }
-                        q_add_shifted<W, DB>(q + cb * DB, v, sh);
+            const uint32_t cur = ds.next(g, last);
+            for (int pass = 0; ok && pass < 2; ++pass) {
+                uint32_t m = pass == 0 ? (cur & ~prev) : (cur & prev);
+                while (m) {
+                    const int blk = __ffs(m) - 1;
+                    m &= m - 1;
+                    OZ_PT(tg);
+                    const bool gotg = mbar_wait(&gfull[blk], static_cast<uint32_t>((fphase >> blk) & 1ull), vabort, TO);
+                    OZ_PADD(pr0, tg);
+                    if (!gotg) {
+                        ok = false;
+                        break;
                     }
-                }
-                if (!last) {
-                    tmem_st_wait();
-                    tc_fence_before();
-                    __syncwarp();
-                    if (lane == 0) mbar_arrive(&gempty[grp]);
+                    fphase ^= (1ull << blk);
+                    tc_fence_after();
+                    OZ_PT(td);
+                    int lo = 0, nb = 0;  // static-index selects (see the MMA issuer)
+#pragma unroll
+                    for (int i = 0; i < kMaxGroups; ++i)
+                        if (i == blk) {
+                            lo = g.blk_lo[i];
+                            nb = g.blk_nb[i];
+                        }
+                    const int hi = lo + nb - 1;
+                    for (int j = lo; j <= hi; ++j) {
+                        const int sh = g.b * (g.J - 1 - j);
+#pragma unroll
+                        for (int cb = 0; cb < HALF / DB; ++cb) {
+                            uint32_t v[DB];
+#pragma unroll
+                            for (int l = 0; l < DB / 8; ++l) tmem_ld8(trow + j * BN + cb * DB + l * 8, v + l * 8);
+                            tmem_ld_wait();
+#pragma unroll
+                            for (int i = 0; i < DB; ++i) reg_fence(v[i]);
+                            q_add_shifted<W, DB>(q + cb * DB, v, sh);
+                        }
+                    }
+                    if (!last) {
+                        tc_fence_before();
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(&gempty[blk]);
+                    }
+                    OZ_PADD(pr1, td);
                 }
             }
+            prev = cur;
         }
         if (!ok && !*vabort) {
             atomicCAS(g.err, 0, DEVERR_TIMEOUT_EPI);
@@ -470,6 +594,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
         }
 
         // ------------------------------------------------------- epilogue
+        OZ_PT(tq);
         if (ok) {
             const int row = mt * BM + 32 * qd + lane;
             const int col0 = nt * BN + half * HALF;
@@ -497,18 +622,28 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                 }
             }
         }
+        OZ_PADD(pr2, tq);
     }
 
     __syncthreads();
+#ifdef OZGB_PROBE
+    if (g.probe && lane == 0 && warp <= 2) {
+        unsigned long long *pp = g.probe + static_cast<size_t>(blockIdx.x) * 8;
+        if (warp == 0) { pp[0] = pr0; pp[7] = clock64() - pstart; }
+        if (warp == 1) { pp[1] = pr0; pp[2] = pr1; pp[3] = pr2; }
+        if (warp == 2) { pp[4] = pr0; pp[5] = pr1; pp[6] = pr2; }
+    }
+    (void)pr3;
+#endif
     if (warp == 1) {
         tc_fence_after();
         tmem_dealloc(tmem, g.tmem_cols);
     }
 }
 
-template <int BN, int W>
+template <int BN, int W, int KC>
 void launch_gemm_variant(const GemmArgs &args, int grid, size_t smem, void *stream) {
-    auto kern = oz_gemm_kernel<BN, W>;
+    auto kern = oz_gemm_kernel<BN, W, KC>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     kern<<<grid, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(args);
 }

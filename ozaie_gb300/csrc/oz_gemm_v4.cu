@@ -1,0 +1,9 @@
+// Kernel variants with 16-column tiles (see oz_gemm.cuh).
+#include "oz_gemm.cuh"
+
+namespace ozgb {
+void launch_gemm_16_4_32(const GemmArgs &a, int g, size_t s, void *st) { launch_gemm_variant<16, 4, 32>(a, g, s, st); }
+void launch_gemm_16_4_16(const GemmArgs &a, int g, size_t s, void *st) { launch_gemm_variant<16, 4, 16>(a, g, s, st); }
+void launch_gemm_16_5_32(const GemmArgs &a, int g, size_t s, void *st) { launch_gemm_variant<16, 5, 32>(a, g, s, st); }
+void launch_gemm_16_5_16(const GemmArgs &a, int g, size_t s, void *st) { launch_gemm_variant<16, 5, 16>(a, g, s, st); }
+}  // namespace ozgb

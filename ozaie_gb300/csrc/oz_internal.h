@@ -22,12 +22,16 @@ namespace ozgb {
 
 constexpr int BM = 128;         // rows of A per tile (UMMA M)
 constexpr int kMaxBins = 64;      // J limit
-constexpr int kMaxGroups = 64;    // drain groups limit
+constexpr int kMaxGroups = 8;     // drain groups limit
 constexpr int kThreads = 320;     // warp 0 producer, warp 1 MMA issuer, warps 2..9 drain + epilogue
 constexpr int kEpiWarps = 8;
 constexpr int kMaxAccWords = 5;
 
 enum OutMode : int { OUT_RN = 0, OUT_RZ_REF = 1, OUT_RAW = 2 };
+
+// Shared memory after the pipeline stages: mbarriers, TMEM slot, abort flag
+// (plus 1 KB of alignment slack).
+constexpr size_t kCtrlBytes = 1024 + 1024;
 
 // Element offset of (row r, k) inside one (rows x KC) canonical block.
 OZ_HD inline long canon_offset(int r, int kk, int KC) {
@@ -44,16 +48,27 @@ struct GemmArgs {
     int32_t *raw;  // OUT_RAW: [M][N][4] words
     int M, N;
     int n_kc, KC, s, J, b;
-    int KBc, G;
-    int bin_lo, bin_hi;
     int out_mode;
     int tiles_m, tiles_n;
     int stages;
-    uint32_t stage_bytes, a_block_bytes, b_block_bytes;
+    // Stage layout: [A: s slices of BM x KC][B region: pad_lo zero slices, the s
+    // loaded B slices, pad_hi zero slices], each B slice BN x KC.
+    uint32_t stage_bytes, a_block_bytes, b_block_bytes, b_pad_lo_bytes, b_region_bytes;
     uint32_t tmem_cols;
     int *err;
     unsigned long long timeout_ns;
-    int grp_lo[kMaxGroups], grp_hi[kMaxGroups];
+    // Per-CTA cycle counters, written only by builds with OZGB_PROBE defined
+    // (8 slots per CTA: producer wait, MMA wait full / wait drained / issue,
+    // drain wait / work, epilogue, total); null otherwise.
+    unsigned long long *probe;
+    // Bin blocks (also the drain groups).  Block g holds bins [lo, lo + nb);
+    // every UMMA of the block covers all of its bins (one accumulator range):
+    // A slice p in [p0, p1] against B slices q = j - p, the out-of-range q
+    // reading zero slices.  Block g is drained after chunk c when
+    // (c + 1 + off) % period == 0, and after the last chunk.
+    int G;
+    int blk_lo[kMaxGroups], blk_nb[kMaxGroups], blk_p0[kMaxGroups], blk_p1[kMaxGroups];
+    int blk_period[kMaxGroups], blk_off[kMaxGroups];
 };
 
 // Device error codes written to the error word.
@@ -62,16 +77,14 @@ enum DevErr : int { DEVERR_NONE = 0, DEVERR_TIMEOUT_PRODUCER = 1, DEVERR_TIMEOUT
 
 typedef void (*GemmLaunchFn)(const GemmArgs &args, int grid, size_t smem, void *stream);
 
-// Kernel variants (tile N x accumulator words); defined in oz_gemm_bn*.cu.
-void launch_gemm_128_2(const GemmArgs &, int, size_t, void *);
-void launch_gemm_64_3(const GemmArgs &, int, size_t, void *);
-void launch_gemm_64_4(const GemmArgs &, int, size_t, void *);
-void launch_gemm_48_3(const GemmArgs &, int, size_t, void *);
-void launch_gemm_48_4(const GemmArgs &, int, size_t, void *);
-void launch_gemm_32_4(const GemmArgs &, int, size_t, void *);
-void launch_gemm_32_5(const GemmArgs &, int, size_t, void *);
-void launch_gemm_16_4(const GemmArgs &, int, size_t, void *);
-void launch_gemm_16_5(const GemmArgs &, int, size_t, void *);
+// Kernel variants: (tile N, exact-accumulator words, K chunk).  Largest tile
+// first; defined in oz_gemm_v*.cu.
+#define OZ_GEMM_VARIANTS(X)                                                                        \
+    X(128, 2, 32) X(128, 2, 16) X(64, 3, 32) X(64, 3, 16) X(64, 4, 32) X(64, 4, 16) X(48, 3, 32)   \
+    X(48, 3, 16) X(48, 4, 32) X(48, 4, 16) X(32, 4, 32) X(32, 4, 16) X(32, 5, 32) X(32, 5, 16)     \
+    X(16, 4, 32) X(16, 4, 16) X(16, 5, 32) X(16, 5, 16)
+#define OZ_DECLARE_GEMM(BN, W, KC) void launch_gemm_##BN##_##W##_##KC(const GemmArgs &, int, size_t, void *);
+OZ_GEMM_VARIANTS(OZ_DECLARE_GEMM)
 
 // Stage (a) / (b) launches (oz_split.cu).
 void launch_rowmax(const double *A, long lda, int M, int K, int32_t *er, double *ss, void *stream);

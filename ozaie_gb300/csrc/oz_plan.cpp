@@ -3,26 +3,25 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
+#include <vector>
 
 namespace ozgb {
 
 namespace {
 
 struct Variant {
-    int BN, W;
+    int BN, W, KC;
     GemmLaunchFn fn;
 };
 
+#define OZ_VARIANT_ENTRY(BN, W, KC) {BN, W, KC, launch_gemm_##BN##_##W##_##KC},
 // Kernel variants, largest tile first.  BN * J <= 512 TMEM columns and the
 // drain registers (BN/2 * W words) bound which ones exist.
-const Variant kVariants[] = {
-    {128, 2, launch_gemm_128_2}, {64, 3, launch_gemm_64_3}, {64, 4, launch_gemm_64_4},
-    {48, 3, launch_gemm_48_3},   {48, 4, launch_gemm_48_4}, {32, 4, launch_gemm_32_4},
-    {32, 5, launch_gemm_32_5},   {16, 4, launch_gemm_16_4}, {16, 5, launch_gemm_16_5},
-};
+const Variant kVariants[] = {OZ_GEMM_VARIANTS(OZ_VARIANT_ENTRY)};
 
 constexpr size_t kSmemLimit = 232448;  // max dynamic shared memory per block on sm_103
-constexpr size_t kSmemReserve = 2048 + 1024;
+constexpr size_t kSmemReserve = kCtrlBytes;
 
 }  // namespace
 
@@ -43,7 +42,7 @@ void reference_table(int K, int mode, int *b, int *d) {
     }
 }
 
-bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string *err) {
+bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string *err, int bin_lo, int bin_hi) {
     Plan p;
     p.cfg = cfg;
     const int b = cfg.b, s = cfg.s, J = cfg.J;
@@ -69,6 +68,11 @@ bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string 
             return false;
         }
     }
+    const int B0 = std::max(0, bin_lo), B1 = std::min(J - 1, bin_hi);
+    if (B0 > B1) {
+        *err = "empty bin range";
+        return false;
+    }
     const double v2 = std::ldexp(1.0, b) - 1.0;
     p.pairs = 0;
     p.max_pairs = 0;
@@ -81,7 +85,7 @@ bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string 
     }
     const int bits = static_cast<int>(std::ceil(std::log2(static_cast<double>(bound) + 1.0))) + 1;
     // K values a bin may accumulate in fp32 between drains: every partial sum
-    // stays an integer of magnitude <= 2^24.
+    // stays an integer of magnitude <= 2^24 (tightest bin).
     const long kb_max = static_cast<long>(std::floor(16777216.0 / (p.max_pairs * v2 * v2)));
     if (kb_max < 16) {
         *err = "too many pairs per bin for exact fp32 accumulation of one 16-deep K step";
@@ -89,6 +93,7 @@ bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string 
     }
     const Variant *chosen = nullptr;
     for (const Variant &v : kVariants) {
+        if (v.KC != 32) continue;
         if (v.BN * J > 512) continue;
         if (32 * v.W < bits) continue;
         chosen = &v;
@@ -101,16 +106,80 @@ bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string 
     }
     p.BN = chosen->BN;
     p.W = chosen->W;
-    p.fn = chosen->fn;
 
+    // ---- bin blocks: contiguous bin ranges of at most 256 columns; every UMMA of a
+    // block spans the whole block (zero B slices pad the out-of-range q).  Measured
+    // on GB300: one M=128 K=16 UMMA costs max(~114, N/2) cycles, so the partition
+    // minimising sum(#A slices x cost(N)) is chosen by dynamic programming.
+    const char *env_g = std::getenv("OZGB_GROUPS");
+    const int max_groups = std::min(kMaxGroups, env_g ? std::max(1, std::atoi(env_g)) : kMaxGroups);
+    const int maxb = 256 / p.BN;
+    auto p0_of = [s](int lo) { return std::max(0, lo - (s - 1)); };
+    auto p1_of = [s](int hi) { return std::min(hi, s - 1); };
+    auto blk_cost = [&](int lo, int hi) {
+        const int nops = p1_of(hi) - p0_of(lo) + 1;
+        return nops * std::max(114.0, (hi - lo + 1) * p.BN / 2.0);
+    };
+    const int nbins = B1 - B0 + 1;
+    const double INF = 1e300;
+    // best[g][i]: min cost covering bins B0 .. B0+i-1 with g blocks
+    std::vector<std::vector<double>> best(max_groups + 1, std::vector<double>(nbins + 1, INF));
+    std::vector<std::vector<int>> from(max_groups + 1, std::vector<int>(nbins + 1, -1));
+    best[0][0] = 0.0;
+    for (int g = 1; g <= max_groups; ++g)
+        for (int i = 1; i <= nbins; ++i)
+            for (int k = std::max(0, i - maxb); k < i; ++k) {
+                if (best[g - 1][k] >= INF) continue;
+                const double c = best[g - 1][k] + blk_cost(B0 + k, B0 + i - 1);
+                if (c < best[g][i]) {
+                    best[g][i] = c;
+                    from[g][i] = k;
+                }
+            }
+    int gbest = -1;
+    for (int g = 1; g <= max_groups; ++g)
+        if (best[g][nbins] < INF && (gbest < 0 || best[g][nbins] < best[gbest][nbins] - 1e-9)) gbest = g;
+    if (gbest < 0) {
+        *err = "bins do not fit " + std::to_string(max_groups) + " blocks of at most 256 columns";
+        return false;
+    }
+    p.model_cycles_per_kstep = best[gbest][nbins];
+    p.G = gbest;
+    {
+        int i = nbins;
+        for (int g = gbest; g >= 1; --g) {
+            const int k = from[g][i];
+            p.blk_lo[g - 1] = B0 + k;
+            p.blk_nb[g - 1] = i - k;
+            i = k;
+        }
+    }
+    p.pad_lo = 0;
+    p.pad_hi = 0;
+    p.mma_per_kstep = 0;
+    for (int g = 0; g < p.G; ++g) {
+        const int lo = p.blk_lo[g], hi = lo + p.blk_nb[g] - 1;
+        p.blk_p0[g] = p0_of(lo);
+        p.blk_p1[g] = p1_of(hi);
+        p.mma_per_kstep += p.blk_p1[g] - p.blk_p0[g] + 1;
+        p.pad_lo = std::max(p.pad_lo, p.blk_p1[g] - lo);           // q = lo - p1 >= -pad_lo
+        p.pad_hi = std::max(p.pad_hi, hi - p.blk_p0[g] - (s - 1));  // q = hi - p0 <= s - 1 + pad_hi
+    }
+
+    // ---- pipeline: K chunk and stage count
     const size_t budget = kSmemLimit - kSmemReserve;
-    const int kc_opts[3] = {64, 32, 16};
+    const int kc_opts[2] = {32, 16};
+    const char *env_kc = std::getenv("OZGB_KC");  // tuning override
+    const int force_kc = env_kc ? std::atoi(env_kc) : 0;
+    auto stage_of = [&](int kc) {
+        return static_cast<size_t>(s) * BM * kc * 2 + static_cast<size_t>(p.pad_lo + s + p.pad_hi) * p.BN * kc * 2;
+    };
     p.KC = 0;
     for (int kc : kc_opts) {
+        if (force_kc && kc != force_kc) continue;
         if (kc > kb_max) continue;
         if (kc > 16 && kc > ((K + 15) / 16) * 16) continue;  // no wider than K needs
-        const size_t stage = static_cast<size_t>(s) * (BM + p.BN) * kc * 2;
-        const size_t st = budget / stage;
+        const size_t st = budget / stage_of(kc);
         if (st >= 2) {
             p.KC = kc;
             p.stages = static_cast<int>(std::min<size_t>(st, 8));
@@ -118,40 +187,55 @@ bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string 
         }
     }
     if (!p.KC) {
-        const size_t stage = static_cast<size_t>(s) * (BM + p.BN) * 16 * 2;
-        if (stage > budget) {
+        if (stage_of(16) > budget) {
             *err = "slices do not fit one 16-deep pipeline stage in shared memory";
             return false;
         }
         p.KC = 16;
         p.stages = 1;
     }
+    p.fn = nullptr;
+    for (const Variant &v : kVariants)
+        if (v.BN == p.BN && v.W == p.W && v.KC == p.KC) p.fn = v.fn;
+    if (!p.fn) {
+        *err = "no kernel variant for this tile / accumulator / K chunk";
+        return false;
+    }
     p.n_kc = (K + p.KC - 1) / p.KC;
     p.Kp = p.n_kc * p.KC;
-    p.KBc = std::max(1, static_cast<int>(kb_max / p.KC));
-    if (p.n_kc <= p.KBc) {
-        p.G = 1;  // no drain before the last chunk
-    } else {
-        p.G = std::min(J, p.KBc);
-    }
-    if (p.G > kMaxGroups) p.G = kMaxGroups;
+
+    // ---- drain periods: bin j may accumulate KB_j K-values in fp32 with
+    // pairs_j * KB_j * (2^b-1)^2 <= 2^24; a block drains at its tightest bin's
+    // period (in chunks).  A period >= n_kc means only after the last chunk.
+    p.min_period = p.n_kc;
     for (int g = 0; g < p.G; ++g) {
-        p.grp_lo[g] = (g * J) / p.G;
-        p.grp_hi[g] = ((g + 1) * J) / p.G - 1;
+        int per = p.n_kc;
+        for (int j = p.blk_lo[g]; j < p.blk_lo[g] + p.blk_nb[g]; ++j) {
+            const long kbj = static_cast<long>(std::floor(16777216.0 / (pairs_in_bin(j, s) * v2 * v2)));
+            per = std::min<long>(per, std::max(1L, kbj / p.KC));
+        }
+        p.blk_period[g] = per;
+        p.min_period = std::min(p.min_period, per);
     }
+    // stagger the drains of different blocks across chunks
+    for (int g = 0; g < p.G; ++g)
+        p.blk_off[g] = (p.blk_period[g] >= p.n_kc) ? 0 : (g * p.blk_period[g]) / std::max(1, p.G);
+
     p.tiles_m = (M + BM - 1) / BM;
     p.tiles_n = (N + p.BN - 1) / p.BN;
     p.Mp = p.tiles_m * BM;
     p.Np = p.tiles_n * p.BN;
+    p.b_slice_bytes = static_cast<uint32_t>(p.BN) * p.KC * 2;
     p.a_block_bytes = static_cast<uint32_t>(s) * BM * p.KC * 2;
-    p.b_block_bytes = static_cast<uint32_t>(s) * p.BN * p.KC * 2;
-    p.stage_bytes = p.a_block_bytes + p.b_block_bytes;
+    p.b_block_bytes = static_cast<uint32_t>(s) * p.b_slice_bytes;
+    p.b_region_bytes = static_cast<uint32_t>(p.pad_lo + s + p.pad_hi) * p.b_slice_bytes;
+    p.stage_bytes = p.a_block_bytes + p.b_region_bytes;
     p.a_elems = static_cast<size_t>(p.tiles_m) * p.n_kc * s * BM * p.KC;
     p.b_elems = static_cast<size_t>(p.tiles_n) * p.n_kc * s * p.BN * p.KC;
     uint32_t cols = 32;
     while (cols < static_cast<uint32_t>(J * p.BN)) cols <<= 1;
     p.tmem_cols = cols;
-    p.smem = static_cast<size_t>(p.stages) * p.stage_bytes + 1024 + 2048;
+    p.smem = static_cast<size_t>(p.stages) * p.stage_bytes + kCtrlBytes;
     *out = p;
     return true;
 }
