@@ -66,7 +66,7 @@ struct ozgb_context {
     Plan last{};
     bool have_last = false;
     // buffers
-    DevBuf a, b, c, at, bt, er, ec, ssr, ssc, err, raw;
+    DevBuf a, b, c, at, bt, er, ec, ssr, ssc, err, raw, knob;
     cudaStream_t stream = nullptr;       // used by the host-array entry points
     cudaStream_t last_stream = nullptr;  // stream of the last enqueued call
     // profiling
@@ -175,18 +175,18 @@ ozgb_status enqueue_exponents(ozgb_handle h, const Operands &o, bool want_ss, cu
 ozgb_status choose_config(ozgb_handle h, const Operands &o, int mode, cudaStream_t st, OzConfig *cfg) {
     *cfg = resolve_config(h, o.K, mode);
     if (h->err_bound > 0.0 && h->opt_slices <= 0) {
-        // precision knob: needs the stage-(a) statistics on the host
-        std::vector<int32_t> er(o.M), ec(o.N);
-        std::vector<double> ssr(o.M), ssc(o.N);
-        cudaMemcpyAsync(er.data(), h->er.p, sizeof(int32_t) * o.M, cudaMemcpyDeviceToHost, st);
-        cudaMemcpyAsync(ec.data(), h->ec.p, sizeof(int32_t) * o.N, cudaMemcpyDeviceToHost, st);
-        cudaMemcpyAsync(ssr.data(), h->ssr.p, sizeof(double) * o.M, cudaMemcpyDeviceToHost, st);
-        cudaMemcpyAsync(ssc.data(), h->ssc.p, sizeof(double) * o.N, cudaMemcpyDeviceToHost, st);
+        // precision knob: the stage-(a) statistics are reduced on the device to the
+        // two spread factors; only those cross to the host
+        if (!h->knob.ensure(2 * sizeof(double))) return fail(h, OZGB_ERR_ALLOC, "knob buffer");
+        launch_knob_rho(static_cast<int32_t *>(h->er.p), static_cast<double *>(h->ssr.p), o.M,
+                        static_cast<int32_t *>(h->ec.p), static_cast<double *>(h->ssc.p), o.N, o.K,
+                        static_cast<double *>(h->knob.p), st);
+        double rho[2] = {1.0, 1.0};
+        cudaMemcpyAsync(rho, h->knob.p, sizeof rho, cudaMemcpyDeviceToHost, st);
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return cuda_fail(h, e, "statistics readback");
         double est = 0;
-        const int s = choose_slices(er.data(), ssr.data(), o.M, ec.data(), ssc.data(), o.N, o.K, cfg->b,
-                                    h->err_bound, 2, 16, &est);
+        const int s = choose_slices_rho(rho[0], rho[1], cfg->b, h->err_bound, 2, 16, &est);
         cfg->s = s;
         cfg->J = s;
     }
@@ -341,7 +341,8 @@ ozgb_status ozgb_release(ozgb_handle h) {
     if (!h) return OZGB_ERR_ARG;
     std::lock_guard<std::mutex> lk(h->mu);
     if (h->device >= 0) cudaSetDevice(h->device);
-    for (DevBuf *b : {&h->a, &h->b, &h->c, &h->at, &h->bt, &h->er, &h->ec, &h->ssr, &h->ssc, &h->raw}) b->release();
+    for (DevBuf *b : {&h->a, &h->b, &h->c, &h->at, &h->bt, &h->er, &h->ec, &h->ssr, &h->ssc, &h->raw, &h->knob})
+        b->release();
     h->setup_done = false;
     return OZGB_OK;
 }

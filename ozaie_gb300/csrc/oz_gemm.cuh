@@ -294,9 +294,10 @@ struct DrainSchedule {
 // ------------------------------------------------------------------ kernel
 template <int BN, int W, int KC>
 __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_constant__ GemmArgs g) {
-    constexpr int HALF = BN / 2;                  // columns per drain thread
-    constexpr int DB = (HALF <= 24) ? HALF : 16;  // columns per TMEM load batch
-    static_assert(HALF % 8 == 0, "BN must be a multiple of 16");
+    constexpr int PARTS = kEpiWarps / 4;          // drain warps sharing one TMEM lane quadrant
+    constexpr int COLS = BN / PARTS;              // columns per drain thread
+    constexpr int DB = (COLS <= 24) ? COLS : 16;  // columns per TMEM load batch
+    static_assert(COLS % 4 == 0 && COLS % DB == 0, "BN must split into 4-column parts");
 
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -525,12 +526,12 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
         // ------------------------------------------ drain + epilogue warps
         const int ew = warp - 2;
         const int qd = warp & 3;  // TMEM lane quadrant accessible to this warp
-        const int half = ew >> 2;
-        const uint32_t trow = tmem + (static_cast<uint32_t>(32 * qd) << 16) + static_cast<uint32_t>(half * HALF);
+        const int part = ew >> 2;  // which COLS-wide column slice of the tile
+        const uint32_t trow = tmem + (static_cast<uint32_t>(32 * qd) << 16) + static_cast<uint32_t>(part * COLS);
 
-        uint32_t q[HALF][W];
+        uint32_t q[COLS][W];
 #pragma unroll
-        for (int i = 0; i < HALF; ++i)
+        for (int i = 0; i < COLS; ++i)
 #pragma unroll
             for (int w = 0; w < W; ++w) q[i][w] = 0;
 
@@ -568,10 +569,9 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                     for (int j = lo; j <= hi; ++j) {
                         const int sh = g.b * (g.J - 1 - j);
 #pragma unroll
-                        for (int cb = 0; cb < HALF / DB; ++cb) {
+                        for (int cb = 0; cb < COLS / DB; ++cb) {
                             uint32_t v[DB];
-#pragma unroll
-                            for (int l = 0; l < DB / 8; ++l) tmem_ld8(trow + j * BN + cb * DB + l * 8, v + l * 8);
+                            tmem_ld_cols<DB>(trow + j * BN + cb * DB, v);
                             tmem_ld_wait();
 #pragma unroll
                             for (int i = 0; i < DB; ++i) reg_fence(v[i]);
@@ -597,13 +597,13 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
         OZ_PT(tq);
         if (ok) {
             const int row = mt * BM + 32 * qd + lane;
-            const int col0 = nt * BN + half * HALF;
+            const int col0 = nt * BN + part * COLS;
             if (row < g.M) {
                 const int er = g.er[row];
                 const int bJ1 = g.b * (g.J + 1);
                 if (g.out_mode == OUT_RAW) {
 #pragma unroll
-                    for (int i = 0; i < HALF; ++i) {
+                    for (int i = 0; i < COLS; ++i) {
                         const int col = col0 + i;
                         if (col < g.N) {
                             int32_t *dst = g.raw + (static_cast<size_t>(row) * g.N + col) * 4;
@@ -615,7 +615,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                 } else {
                     double *crow = g.c + static_cast<size_t>(row) * g.ldc;
 #pragma unroll
-                    for (int i = 0; i < HALF; ++i) {
+                    for (int i = 0; i < COLS; ++i) {
                         const int col = col0 + i;
                         if (col < g.N) crow[col] = q_to_double<W>(q[i], er + g.ec[col], bJ1, g.out_mode);
                     }

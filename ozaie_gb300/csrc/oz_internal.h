@@ -23,8 +23,8 @@ namespace ozgb {
 constexpr int BM = 128;         // rows of A per tile (UMMA M)
 constexpr int kMaxBins = 64;      // J limit
 constexpr int kMaxGroups = 8;     // drain groups limit
-constexpr int kThreads = 320;     // warp 0 producer, warp 1 MMA issuer, warps 2..9 drain + epilogue
-constexpr int kEpiWarps = 8;
+constexpr int kEpiWarps = 16;     // drain + epilogue warps: 4 per TMEM lane quadrant
+constexpr int kThreads = 64 + 32 * kEpiWarps;  // warp 0 producer, warp 1 MMA issuer, then the drain warps
 constexpr int kMaxAccWords = 5;
 
 enum OutMode : int { OUT_RN = 0, OUT_RZ_REF = 1, OUT_RAW = 2 };
@@ -94,5 +94,9 @@ void launch_split_a(const double *A, long lda, int M, int K, const int32_t *er, 
 void launch_split_b(const double *B, long ldb, int K, int N, const int32_t *ec, int b, int s, int KC, int n_kc,
                     int BN, int Np, uint16_t *tiles, void *stream);
 int launch_selftest_timeout(int *err, unsigned long long timeout_ns, void *stream);
+// Precision-knob statistics: rho[0] = rho_A over the rows of A, rho[1] = rho_B over
+// the columns of B, rho^2 = sum 4^{E-1022} / sum(|x|^2 / K).
+void launch_knob_rho(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N, int K,
+                     double *rho, void *stream);
 
 }  // namespace ozgb

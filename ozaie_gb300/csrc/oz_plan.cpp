@@ -260,6 +260,10 @@ int choose_slices(const int32_t *er, const double *ssr, int M, const int32_t *ec
         return static_cast<double>(std::sqrt(num / den));
     };
     const double ra = rho(er, ssr, M), rb = rho(ec, ssc, N);
+    return choose_slices_rho(ra, rb, b, bound, s_min, s_max, estimate);
+}
+
+int choose_slices_rho(double ra, double rb, int b, double bound, int s_min, int s_max, double *estimate) {
     const double safety = 2.0;
     int s = s_min;
     double est = 0.0;

@@ -53,5 +53,8 @@ void reference_table(int K, int mode, int *b, int *d);
 // writes the a-priori estimate for it.
 int choose_slices(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N, int K,
                   int b, double bound, int s_min, int s_max, double *estimate);
+// The same rule from the two spread factors rho_A, rho_B (computed on the device
+// by launch_knob_rho, or on the host by choose_slices).
+int choose_slices_rho(double ra, double rb, int b, double bound, int s_min, int s_max, double *estimate);
 
 }  // namespace ozgb

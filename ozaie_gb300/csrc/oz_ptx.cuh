@@ -110,6 +110,19 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t *r) {
         : "r"(taddr)
         : "memory");
 }
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, uint32_t *r) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(taddr)
+                 : "memory");
+}
+// N consecutive columns (N a multiple of 4) of this thread's TMEM lane.
+template <int N>
+__device__ __forceinline__ void tmem_ld_cols(uint32_t taddr, uint32_t *r) {
+#pragma unroll
+    for (int l = 0; l < N / 8; ++l) tmem_ld8(taddr + l * 8, r + l * 8);
+    if constexpr (N % 8 == 4) tmem_ld4(taddr + (N / 8) * 8, r + (N / 8) * 8);
+}
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void tmem_st8_zero(uint32_t taddr) {
     const uint32_t z = 0;

@@ -193,7 +193,61 @@ __global__ void k_selftest_timeout(int *err, unsigned long long timeout_ns) {
     }
 }
 
+// Precision-knob spread factor of one side (block 0: rows of A, block 1: columns
+// of B): rho^2 = sum_i 4^{E_i-1022} / sum_i (ss_i / K), scaled by the max exponent.
+__global__ void k_knob_rho(const int32_t *__restrict__ er, const double *__restrict__ ssr, int M,
+                           const int32_t *__restrict__ ec, const double *__restrict__ ssc, int N, int K,
+                           double *__restrict__ rho) {
+    const int32_t *e = blockIdx.x == 0 ? er : ec;
+    const double *ss = blockIdx.x == 0 ? ssr : ssc;
+    const int n = blockIdx.x == 0 ? M : N;
+    __shared__ int s_max[32];
+    __shared__ double s_num[32], s_den[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int emax = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) emax = max(emax, e[i]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+    if (lane == 0) s_max[wid] = emax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int m = 0;
+        for (int w = 0; w < nw; ++w) m = max(m, s_max[w]);
+        s_max[0] = m;
+    }
+    __syncthreads();
+    emax = s_max[0];
+    double num = 0.0, den = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        num += ldexp(1.0, 2 * (e[i] - emax));
+        den += ldexp(ss[i] / K, -2 * (emax - 1022));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        num += __shfl_xor_sync(0xffffffffu, num, o);
+        den += __shfl_xor_sync(0xffffffffu, den, o);
+    }
+    if (lane == 0) {
+        s_num[wid] = num;
+        s_den[wid] = den;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int w = 0; w < nw; ++w) {
+            a += s_num[w];
+            b += s_den[w];
+        }
+        rho[blockIdx.x] = (b > 0.0) ? sqrt(a / b) : 1.0;
+    }
+}
+
 // ---------------------------------------------------------------- launches
+void launch_knob_rho(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N, int K,
+                     double *rho, void *stream) {
+    k_knob_rho<<<2, 1024, 0, static_cast<cudaStream_t>(stream)>>>(er, ssr, M, ec, ssc, N, K, rho);
+}
+
 void launch_rowmax(const double *A, long lda, int M, int K, int32_t *er, double *ss, void *stream) {
     const int threads = 256;
     const int blocks = (M * 32 + threads - 1) / threads;
