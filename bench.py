@@ -65,7 +65,7 @@ def profile_traffic():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms."""
 
     def __init__(self, index):
         self.index = index
@@ -78,7 +78,7 @@ class ClockSampler:
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
@@ -179,7 +179,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -275,9 +275,12 @@ def main():
 
     clocks = ClockSampler(local)
     clocks.start()
+    for _ in range(max(3, args.warmup)):  # keeps the GPU busy while the sampler starts
+        step()
     if ws > 1:
         dist.barrier()
     torch.cuda.synchronize()
+    n_launch0 = h.launch_count()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -288,6 +291,7 @@ def main():
     if ws > 1:
         dist.barrier()
     ms = e0.elapsed_time(e1) / args.steps
+    gpu_launches = h.launch_count() - n_launch0
     clk = clocks.stop()
     if h.sync():
         raise RuntimeError(h.last_error())
@@ -299,16 +303,19 @@ def main():
     value = flops * ws / (ms * 1e-3) / 1e12
 
     # e2e: host arrays through the reference-facing call, copies inside the timed region
+    # inputs and result in pinned host memory, as a caller streaming many products would keep them
+    A_host = torch.from_numpy(A).pin_memory().numpy()
+    B_host = torch.from_numpy(B).pin_memory().numpy()
     he = oz.Handle()
     he.set_error_bound(BOUND)
     assert he.setup(M, N, K, oz.Mode.fast) == 0, he.last_error()
-    Ch = np.empty((M, N))
+    Ch = torch.empty((M, N), dtype=torch.float64).pin_memory().numpy()
     for _ in range(2):
-        assert he.dgemm(M, N, K, A, B, Ch) == 0, he.last_error()
+        assert he.dgemm(M, N, K, A_host, B_host, Ch) == 0, he.last_error()
     e2e_steps = max(3, min(args.steps, 10))
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        assert he.dgemm(M, N, K, A, B, Ch) == 0, he.last_error()
+        assert he.dgemm(M, N, K, A_host, B_host, Ch) == 0, he.last_error()
     e2e_ms = (time.perf_counter() - t0) / e2e_steps * 1e3
     he.close()
 
@@ -354,7 +361,7 @@ def main():
                          "frac": achieved / peaks["bf16_tflops"], "traffic": traffic,
                          "peak_source": peaks["source"] + " bf16 burst (cuBLAS)",
                          "algorithmic": "2 * pairs * M * N * K bf16 MMA flops per launch"},
-            "gpu_launches": 5 * args.steps,
+            "gpu_launches": gpu_launches,
             "clocks": clk,
         }
         if not args.no_cpu_baseline:

@@ -129,6 +129,9 @@ ozgb_status ozgb_get_config(ozgb_handle h, ozgb_config *out);
  * [2] slice-pair GEMM + accumulation, [3] total.  Needs ozgb_set_profiling(h, 1). */
 ozgb_status ozgb_set_profiling(ozgb_handle h, int enable);
 ozgb_status ozgb_stage_times(ozgb_handle h, float *ms, int n);
+/* Number of kernels this handle has launched so far (all entry points).  No
+ * reference counterpart: lets a caller check that its calls ran on the GPU. */
+ozgb_status ozgb_launch_count(ozgb_handle h, long long *count);
 const char *ozgb_last_error(ozgb_handle h);
 
 /* -------------------------------------------------------- test / debug hooks */
@@ -155,11 +158,17 @@ ozgb_status ozgb_convert_paired_i64_to_double(const int64_t *C, double *result, 
 /* Host-only planning query (no device needed): the kernel configuration the
  * library would use for an M x N x K product with `bits`, `slices`, `bins`. */
 int ozgb_plan_query(int M, int N, int K, int bits, int slices, int bins, ozgb_config *out);
-/* Host-only precision knob (no device needed): the smallest slice count whose
- * a-priori normwise error estimate is <= bound, from the stage-(a) statistics
- * (row/column max exponents and sums of squares).  Returns -1 on bad input. */
+/* Host-only precision knob (no device needed): the smallest slice count in
+ * [2, 16] whose a-priori normwise error estimate is <= bound (16 if none), from
+ * the stage-(a) statistics: row max exponent fields er and row sums of squares
+ * ssr of A, column fields ec and column sums of squares ssc of B, and the sums
+ * of squares along k, sa_k[k] = |A(:,k)|^2 and sb_k[k] = |B(k,:)|^2 (both may be
+ * NULL: the mass of A and B is then taken as spread evenly over k).  The
+ * device path computes the same statistics itself.  No reference counterpart:
+ * the reference fixes s per shape (include/oz_aie.h:60-80).  Returns -1 on bad
+ * input. */
 int ozgb_choose_slices(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N,
-                       int K, int bits, double bound, double *estimate);
+                       const double *sa_k, const double *sb_k, int K, int bits, double bound, double *estimate);
 
 /* Library version string. */
 const char *ozgb_version(void);

@@ -86,7 +86,8 @@ SIGNATURES = [
     ("ozgb_selftest_timeout", _i, [_h, _dbl]),
     ("ozgb_convert_paired_i64_to_double", _i, [_p, _p, _i, _i, _i, _i, _i]),
     ("ozgb_plan_query", _i, [_i, _i, _i, _i, _i, _i, ctypes.POINTER(OzgbConfig)]),
-    ("ozgb_choose_slices", _i, [_p, _p, _i, _p, _p, _i, _i, _i, _dbl, ctypes.POINTER(_dbl)]),
+    ("ozgb_choose_slices", _i, [_p, _p, _i, _p, _p, _i, _p, _p, _i, _i, _dbl, ctypes.POINTER(_dbl)]),
+    ("ozgb_launch_count", _i, [_h, ctypes.POINTER(ctypes.c_longlong)]),
     ("ozgb_version", ctypes.c_char_p, []),
 ]
 

@@ -146,6 +146,11 @@ class Handle:
         self._check(self._L.ozgb_stage_times(self._h, t, 4))
         return {"exponents": t[0], "split": t[1], "gemm": t[2], "total": t[3]}
 
+    def launch_count(self):
+        n = ctypes.c_longlong()
+        self._check(self._L.ozgb_launch_count(self._h, ctypes.byref(n)))
+        return n.value
+
     def config(self):
         c = OzgbConfig()
         self._check(self._L.ozgb_get_config(self._h, ctypes.byref(c)))
@@ -200,14 +205,20 @@ def plan_query(M, N, K, bits, slices, bins):
     return None if rc else c.as_dict()
 
 
-def choose_slices(er, ssr, ec, ssc, K, bits, bound):
+def choose_slices(er, ssr, ec, ssc, K, bits, bound, sa_k=None, sb_k=None):
+    """Host-only precision knob: (slice count, a-priori error estimate) for a
+    requested normwise bound, from the stage-(a) statistics.  sa_k / sb_k are the
+    sums of squares of the columns of A and the rows of B (None: spread evenly)."""
     er = np.ascontiguousarray(er, np.int32)
     ec = np.ascontiguousarray(ec, np.int32)
     ssr = np.ascontiguousarray(ssr, np.float64)
     ssc = np.ascontiguousarray(ssc, np.float64)
+    ka = None if sa_k is None else np.ascontiguousarray(sa_k, np.float64)
+    kb = None if sb_k is None else np.ascontiguousarray(sb_k, np.float64)
     est = ctypes.c_double()
-    s = load().ozgb_choose_slices(_ptr(er), _ptr(ssr), er.size, _ptr(ec), _ptr(ssc), ec.size, int(K), int(bits),
-                                  float(bound), ctypes.byref(est))
+    s = load().ozgb_choose_slices(_ptr(er), _ptr(ssr), er.size, _ptr(ec), _ptr(ssc), ec.size,
+                                  None if ka is None else _ptr(ka), None if kb is None else _ptr(kb), int(K),
+                                  int(bits), float(bound), ctypes.byref(est))
     return s, est.value
 
 

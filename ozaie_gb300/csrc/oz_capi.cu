@@ -66,13 +66,14 @@ struct ozgb_context {
     Plan last{};
     bool have_last = false;
     // buffers
-    DevBuf a, b, c, at, bt, er, ec, ssr, ssc, err, raw, knob;
+    DevBuf a, b, c, at, bt, er, ec, ssr, ssc, err, raw, knob, kca, krb, ktmp;
     cudaStream_t stream = nullptr;       // used by the host-array entry points
     cudaStream_t last_stream = nullptr;  // stream of the last enqueued call
     // profiling
     bool profiling = false;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     bool ev_recorded = false;
+    long long launches = 0;  // kernels this handle has launched
     std::string msg;
 };
 
@@ -169,24 +170,36 @@ ozgb_status enqueue_exponents(ozgb_handle h, const Operands &o, bool want_ss, cu
     cudaMemsetAsync(h->ec.p, 0, sizeof(int32_t) * o.N, st);
     launch_rowmax(o.A, o.lda, o.M, o.K, static_cast<int32_t *>(h->er.p), ssr, st);
     launch_colmax(o.B, o.ldb, o.K, o.N, static_cast<int32_t *>(h->ec.p), ssc, st);
+    h->launches += 2;
     return OZGB_OK;
 }
 
 ozgb_status choose_config(ozgb_handle h, const Operands &o, int mode, cudaStream_t st, OzConfig *cfg) {
     *cfg = resolve_config(h, o.K, mode);
     if (h->err_bound > 0.0 && h->opt_slices <= 0) {
-        // precision knob: the stage-(a) statistics are reduced on the device to the
-        // two spread factors; only those cross to the host
-        if (!h->knob.ensure(2 * sizeof(double))) return fail(h, OZGB_ERR_ALLOC, "knob buffer");
-        launch_knob_rho(static_cast<int32_t *>(h->er.p), static_cast<double *>(h->ssr.p), o.M,
-                        static_cast<int32_t *>(h->ec.p), static_cast<double *>(h->ssc.p), o.N, o.K,
-                        static_cast<double *>(h->knob.p), st);
-        double rho[2] = {1.0, 1.0};
-        cudaMemcpyAsync(rho, h->knob.p, sizeof rho, cudaMemcpyDeviceToHost, st);
+        // precision knob: besides the stage-(a) row/column statistics it needs the
+        // sums of squares along k (columns of A, rows of B), which two more passes
+        // of the same reduction kernels give; everything is reduced on the device to
+        // five scaled sums, and only those cross to the host
+        if (!h->knob.ensure(5 * sizeof(double)) || !h->kca.ensure(sizeof(double) * o.K) ||
+            !h->krb.ensure(sizeof(double) * o.K) || !h->ktmp.ensure(sizeof(int32_t) * o.K))
+            return fail(h, OZGB_ERR_ALLOC, "knob buffers");
+        double *ca = static_cast<double *>(h->kca.p), *rb = static_cast<double *>(h->krb.p);
+        int32_t *tmp = static_cast<int32_t *>(h->ktmp.p);
+        cudaMemsetAsync(ca, 0, sizeof(double) * o.K, st);
+        cudaMemsetAsync(tmp, 0, sizeof(int32_t) * o.K, st);
+        launch_colmax(o.A, o.lda, o.M, o.K, tmp, ca, st);
+        launch_rowmax(o.B, o.ldb, o.K, o.N, tmp, rb, st);
+        launch_knob_stats(static_cast<int32_t *>(h->er.p), static_cast<double *>(h->ssr.p), o.M,
+                          static_cast<int32_t *>(h->ec.p), static_cast<double *>(h->ssc.p), o.N, ca, rb, o.K,
+                          static_cast<double *>(h->knob.p), st);
+        h->launches += 3;
+        KnobStats ks;
+        cudaMemcpyAsync(&ks, h->knob.p, sizeof ks, cudaMemcpyDeviceToHost, st);
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return cuda_fail(h, e, "statistics readback");
         double est = 0;
-        const int s = choose_slices_rho(rho[0], rho[1], cfg->b, h->err_bound, 2, 16, &est);
+        const int s = choose_slices_stats(ks, o.K, cfg->b, h->err_bound, 2, 16, &est);
         cfg->s = s;
         cfg->J = s;
     }
@@ -202,6 +215,7 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
     launch_split_a(o.A, o.lda, o.M, o.K, static_cast<int32_t *>(h->er.p), p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.Mp, at, st);
     launch_split_b(o.B, o.ldb, o.K, o.N, static_cast<int32_t *>(h->ec.p), p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.BN, p.Np,
                    bt, st);
+    h->launches += 2;
     if (h->profiling) cudaEventRecord(h->ev[2], st);
     GemmArgs g;
     memset(&g, 0, sizeof g);
@@ -254,6 +268,7 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
     g.probe = probe;
 #endif
     p.fn(g, p.tiles_m * p.tiles_n, p.smem, st);
+    h->launches += 1;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(h, e, "slice-pair GEMM launch");
 #ifdef OZGB_PROBE
@@ -341,7 +356,8 @@ ozgb_status ozgb_release(ozgb_handle h) {
     if (!h) return OZGB_ERR_ARG;
     std::lock_guard<std::mutex> lk(h->mu);
     if (h->device >= 0) cudaSetDevice(h->device);
-    for (DevBuf *b : {&h->a, &h->b, &h->c, &h->at, &h->bt, &h->er, &h->ec, &h->ssr, &h->ssc, &h->raw, &h->knob})
+    for (DevBuf *b : {&h->a, &h->b, &h->c, &h->at, &h->bt, &h->er, &h->ec, &h->ssr, &h->ssc, &h->raw, &h->knob, &h->kca,
+                      &h->krb, &h->ktmp})
         b->release();
     h->setup_done = false;
     return OZGB_OK;
@@ -526,6 +542,13 @@ ozgb_status ozgb_stage_times(ozgb_handle h, float *ms, int n) {
     return OZGB_OK;
 }
 
+ozgb_status ozgb_launch_count(ozgb_handle h, long long *count) {
+    if (!h || !count) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    *count = h->launches;
+    return OZGB_OK;
+}
+
 ozgb_status ozgb_get_config(ozgb_handle h, ozgb_config *out) {
     if (!h || !out) return OZGB_ERR_ARG;
     std::lock_guard<std::mutex> lk(h->mu);
@@ -611,6 +634,7 @@ ozgb_status ozgb_selftest_timeout(ozgb_handle h, double timeout_ms) {
     if (rc) return rc;
     launch_selftest_timeout(static_cast<int *>(h->err.p), static_cast<unsigned long long>(timeout_ms * 1e6),
                             h->stream);
+    h->launches += 1;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(h, e, "selftest launch");
     return check_device_error(h, h->stream);
@@ -669,15 +693,16 @@ int ozgb_plan_query(int M, int N, int K, int bits, int slices, int bins, ozgb_co
         out->drain_chunks = p.min_period;
         out->acc_words = p.W;
         out->pairs = p.pairs;
-    fill_blocks(p, out);
+        fill_blocks(p, out);
     }
     return OZGB_OK;
 }
 
-int ozgb_choose_slices(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N, int K,
-                       int bits, double bound, double *estimate) {
+int ozgb_choose_slices(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N,
+                       const double *sa_k, const double *sb_k, int K, int bits, double bound, double *estimate) {
     if (!er || !ssr || !ec || !ssc || M < 1 || N < 1 || K < 1 || bits < 1 || !(bound > 0)) return -1;
-    return choose_slices(er, ssr, M, ec, ssc, N, K, bits, bound, 2, 16, estimate);
+    const KnobStats ks = knob_stats_host(er, ssr, M, ec, ssc, N, sa_k, sb_k, K);
+    return choose_slices_stats(ks, K, bits, bound, 2, 16, estimate);
 }
 
 }  // extern "C"

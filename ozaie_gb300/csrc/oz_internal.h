@@ -94,9 +94,10 @@ void launch_split_a(const double *A, long lda, int M, int K, const int32_t *er, 
 void launch_split_b(const double *B, long ldb, int K, int N, const int32_t *ec, int b, int s, int KC, int n_kc,
                     int BN, int Np, uint16_t *tiles, void *stream);
 int launch_selftest_timeout(int *err, unsigned long long timeout_ns, void *stream);
-// Precision-knob statistics: rho[0] = rho_A over the rows of A, rho[1] = rho_B over
-// the columns of B, rho^2 = sum 4^{E-1022} / sum(|x|^2 / K).
-void launch_knob_rho(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N, int K,
-                     double *rho, void *stream);
+// Precision-knob statistics (five doubles, see KnobStats in oz_plan.h) from the
+// row/column exponents and sums of squares of stage (a) and the per-k sums of
+// squares ca[k] = |A(:,k)|^2, rb[k] = |B(k,:)|^2.
+void launch_knob_stats(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N,
+                       const double *ca, const double *rb, int K, double *out, void *stream);
 
 }  // namespace ozgb

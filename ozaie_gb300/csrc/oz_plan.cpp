@@ -240,40 +240,50 @@ bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string 
     return true;
 }
 
-int choose_slices(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N, int K,
-                  int b, double bound, int s_min, int s_max, double *estimate) {
-    // Dropped pairs p + q = s dominate the error of the triangular set: each is a
-    // product of two digits of rms ~0.57 * 2^b at weights 2^{E-1022-b(p+1)}, summed
-    // over s-1 pairs with random signs.  The truncated tails add ~0.58 2^{-bs} per
-    // operand.  Relative to the rms size of C this gives, with
-    // rho_A^2 = sum_i 4^{Er_i-1022} / sum_i (|a_i|^2 / K) and rho_B likewise,
-    //   est(s) = 2^{-bs} (0.33 sqrt(s-1) rho_A rho_B + 0.58 (rho_A + rho_B)).
-    auto rho = [K](const int32_t *e, const double *ss, int n) {
-        int emax = 0;
-        for (int i = 0; i < n; ++i) emax = std::max(emax, static_cast<int>(e[i]));
-        long double num = 0.0L, den = 0.0L;
-        for (int i = 0; i < n; ++i) {
-            num += std::ldexp(1.0L, 2 * (e[i] - emax));
-            den += std::ldexp(static_cast<long double>(ss[i]) / K, -2 * (emax - 1022));
-        }
-        if (den <= 0.0L) return 1.0;
-        return static_cast<double>(std::sqrt(num / den));
-    };
-    const double ra = rho(er, ssr, M), rb = rho(ec, ssc, N);
-    return choose_slices_rho(ra, rb, b, bound, s_min, s_max, estimate);
+double knob_estimate(const KnobStats &k, int K, int b, int s) {
+    const double safety = 1.5;
+    if (!(k.t > 0.0)) return HUGE_VAL;
+    const double dropped = 0.25 * (s - 1.0) * std::sqrt(static_cast<double>(K) * k.sa * k.sb);
+    const double tails = std::sqrt(k.sa * k.nb / 3.0) + std::sqrt(k.sb * k.na / 3.0);
+    const double v = safety * std::ldexp((dropped + tails) / std::sqrt(k.t), -b * s) + std::ldexp(1.0, -53);
+    return std::isfinite(v) ? v : HUGE_VAL;
 }
 
-int choose_slices_rho(double ra, double rb, int b, double bound, int s_min, int s_max, double *estimate) {
-    const double safety = 2.0;
+int choose_slices_stats(const KnobStats &k, int K, int b, double bound, int s_min, int s_max, double *estimate) {
     int s = s_min;
-    double est = 0.0;
-    for (s = s_min; s <= s_max; ++s) {
-        est = safety * std::ldexp(0.33 * std::sqrt(std::max(1.0, s - 1.0)) * ra * rb + 0.58 * (ra + rb), -b * s);
+    double est = HUGE_VAL;
+    for (; s <= s_max; ++s) {
+        est = knob_estimate(k, K, b, s);
         if (est <= bound) break;
     }
     if (s > s_max) s = s_max;
     if (estimate) *estimate = est;
     return s;
+}
+
+KnobStats knob_stats_host(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N,
+                          const double *ca, const double *rb, int K) {
+    int ea = 0, eb = 0;
+    for (int i = 0; i < M; ++i) ea = std::max(ea, static_cast<int>(er[i]));
+    for (int j = 0; j < N; ++j) eb = std::max(eb, static_cast<int>(ec[j]));
+    long double sa = 0, na = 0, sb = 0, nb = 0, t = 0;
+    for (int i = 0; i < M; ++i) {
+        sa += std::ldexp(1.0L, 2 * (er[i] - ea));
+        na += std::ldexp(static_cast<long double>(ssr[i]), -2 * (ea - 1022));
+    }
+    for (int j = 0; j < N; ++j) {
+        sb += std::ldexp(1.0L, 2 * (ec[j] - eb));
+        nb += std::ldexp(static_cast<long double>(ssc[j]), -2 * (eb - 1022));
+    }
+    if (ca && rb) {
+        for (int k = 0; k < K; ++k)
+            t += std::ldexp(static_cast<long double>(ca[k]), -2 * (ea - 1022)) *
+                 std::ldexp(static_cast<long double>(rb[k]), -2 * (eb - 1022));
+    } else {
+        t = na * nb / K;
+    }
+    return KnobStats{static_cast<double>(sa), static_cast<double>(na), static_cast<double>(sb),
+                     static_cast<double>(nb), static_cast<double>(t)};
 }
 
 }  // namespace ozgb

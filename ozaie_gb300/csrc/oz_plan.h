@@ -48,13 +48,39 @@ bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string 
 // The reference's (b, d) tables, include/oz_aie.h:60-80, indexed by log2 K.
 void reference_table(int K, int mode, int *b, int *d);
 
-// Slice count for a requested normwise relative error, from the stage-(a)
-// statistics (max exponents and sums of squares).  Returns the chosen s and
-// writes the a-priori estimate for it.
-int choose_slices(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N, int K,
-                  int b, double bound, int s_min, int s_max, double *estimate);
-// The same rule from the two spread factors rho_A, rho_B (computed on the device
-// by launch_knob_rho, or on the host by choose_slices).
-int choose_slices_rho(double ra, double rb, int b, double bound, int s_min, int s_max, double *estimate);
+// Precision-knob statistics, scaled by the largest row exponent ea of A and the
+// largest column exponent eb of B:
+//   sa = sum_i 4^{Er_i-ea},  na = ||A||_F^2 4^{1022-ea},
+//   sb = sum_j 4^{Ec_j-eb},  nb = ||B||_F^2 4^{1022-eb},
+//   t  = sum_k |A(:,k)|^2 |B(k,:)|^2 4^{2044-ea-eb}  (E||AB||_F^2 for random signs).
+struct KnobStats {
+    double sa, na, sb, nb, t;
+};
+
+// A-priori normwise relative error of the triangular pair set with s slices of
+// b bits.  Write x = 2^{E-1022} (sum_p x_p 2^{-b(p+1)} + r 2^{-bs}) with digits
+// x_p in [0, 2^b) and a truncated tail r in [0, 1).  For one product a b the
+// error of the kept pairs p+q <= s-1 is 2^{Er+Ec-2044-bs} ((s-1)/4 + r_a beta +
+// r_b alpha) to first order: the s-1 dropped pairs p+q = s (mean digit product
+// 4^b/4, all of the product's sign) and the two tails (alpha, beta the scaled
+// magnitudes).  Summing over k with random signs, over C, and bounding the
+// three terms separately (Minkowski):
+//   est(s) = 1.5 2^{-bs} ((s-1)/4 sqrt(K sa sb) + sqrt(sa nb / 3) + sqrt(sb na / 3)) / sqrt(t)
+//            + 2^{-53} (rounding of the result).
+// For phi <= 1 inputs the unscaled model is within a few percent of the
+// measured error; heavier tails make it conservative.  Non-finite or zero
+// statistics give an infinite estimate (the caller then takes its largest s).
+double knob_estimate(const KnobStats &k, int K, int b, int s);
+
+// Slice count for a requested normwise relative error: the smallest s in
+// [s_min, s_max] with knob_estimate <= bound (s_max if none).  Writes the
+// estimate for the returned s.
+int choose_slices_stats(const KnobStats &k, int K, int b, double bound, int s_min, int s_max, double *estimate);
+
+// KnobStats computed on the host from stage-(a) style statistics.  ca/rb (the
+// per-k sums of squares of the columns of A and the rows of B) may be null:
+// t then falls back to ||A||^2 ||B||^2 / K (mass spread evenly over k).
+KnobStats knob_stats_host(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N,
+                          const double *ca, const double *rb, int K);
 
 }  // namespace ozgb

@@ -193,59 +193,81 @@ __global__ void k_selftest_timeout(int *err, unsigned long long timeout_ns) {
     }
 }
 
-// Precision-knob spread factor of one side (block 0: rows of A, block 1: columns
-// of B): rho^2 = sum_i 4^{E_i-1022} / sum_i (ss_i / K), scaled by the max exponent.
-__global__ void k_knob_rho(const int32_t *__restrict__ er, const double *__restrict__ ssr, int M,
-                           const int32_t *__restrict__ ec, const double *__restrict__ ssc, int N, int K,
-                           double *__restrict__ rho) {
-    const int32_t *e = blockIdx.x == 0 ? er : ec;
-    const double *ss = blockIdx.x == 0 ? ssr : ssc;
-    const int n = blockIdx.x == 0 ? M : N;
-    __shared__ int s_max[32];
-    __shared__ double s_num[32], s_den[32];
+// Block-wide reductions over blockDim.x threads (a multiple of 32, at most 1024).
+__device__ int block_max_int(int v, int *sh) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    int emax = 0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) emax = max(emax, e[i]);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
-    if (lane == 0) s_max[wid] = emax;
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
     __syncthreads();
-    if (threadIdx.x == 0) {
-        int m = 0;
-        for (int w = 0; w < nw; ++w) m = max(m, s_max[w]);
-        s_max[0] = m;
-    }
+    if (lane == 0) sh[wid] = v;
     __syncthreads();
-    emax = s_max[0];
-    double num = 0.0, den = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        num += ldexp(1.0, 2 * (e[i] - emax));
-        den += ldexp(ss[i] / K, -2 * (emax - 1022));
-    }
+    int m = sh[0];
+    for (int w = 1; w < nw; ++w) m = max(m, sh[w]);
+    return m;
+}
+
+__device__ double block_sum(double v, double *sh) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        num += __shfl_xor_sync(0xffffffffu, num, o);
-        den += __shfl_xor_sync(0xffffffffu, den, o);
-    }
-    if (lane == 0) {
-        s_num[wid] = num;
-        s_den[wid] = den;
-    }
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double a = 0.0, b = 0.0;
-        for (int w = 0; w < nw; ++w) {
-            a += s_num[w];
-            b += s_den[w];
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    double s = 0.0;
+    for (int w = 0; w < nw; ++w) s += sh[w];
+    return s;
+}
+
+// Precision-knob statistics, all scaled by the largest row exponent ea of A and
+// the largest column exponent eb of B so that they stay in range:
+//   out[0] = sum_i 4^{Er_i-ea}           out[1] = sum_i |a_i|^2 4^{1022-ea}
+//   out[2] = sum_j 4^{Ec_j-eb}           out[3] = sum_j |b_j|^2 4^{1022-eb}
+//   out[4] = sum_k |A(:,k)|^2 |B(k,:)|^2 4^{2044-ea-eb}
+// Block 0 makes the A terms, block 1 the B terms, block 2 the K-direction term.
+__global__ void k_knob_stats(const int32_t *__restrict__ er, const double *__restrict__ ssr, int M,
+                             const int32_t *__restrict__ ec, const double *__restrict__ ssc, int N,
+                             const double *__restrict__ ca, const double *__restrict__ rb, int K,
+                             double *__restrict__ out) {
+    __shared__ int sh_i[32];
+    __shared__ double sh_d[32];
+    int ea = 0, eb = 0;
+    if (blockIdx.x != 1) {
+        for (int i = threadIdx.x; i < M; i += blockDim.x) ea = max(ea, er[i]);
+        ea = block_max_int(ea, sh_i);
+    }
+    if (blockIdx.x != 0) {
+        for (int j = threadIdx.x; j < N; j += blockDim.x) eb = max(eb, ec[j]);
+        eb = block_max_int(eb, sh_i);
+    }
+    if (blockIdx.x < 2) {
+        const int32_t *e = blockIdx.x == 0 ? er : ec;
+        const double *ss = blockIdx.x == 0 ? ssr : ssc;
+        const int n = blockIdx.x == 0 ? M : N;
+        const int emax = blockIdx.x == 0 ? ea : eb;
+        double num = 0.0, den = 0.0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            num += ldexp(1.0, 2 * (e[i] - emax));
+            den += ldexp(ss[i], -2 * (emax - 1022));
         }
-        rho[blockIdx.x] = (b > 0.0) ? sqrt(a / b) : 1.0;
+        num = block_sum(num, sh_d);
+        den = block_sum(den, sh_d);
+        if (threadIdx.x == 0) {
+            out[2 * blockIdx.x] = num;
+            out[2 * blockIdx.x + 1] = den;
+        }
+    } else {
+        double t = 0.0;
+        for (int k = threadIdx.x; k < K; k += blockDim.x)
+            t += ldexp(ca[k], -2 * (ea - 1022)) * ldexp(rb[k], -2 * (eb - 1022));
+        t = block_sum(t, sh_d);
+        if (threadIdx.x == 0) out[4] = t;
     }
 }
 
 // ---------------------------------------------------------------- launches
-void launch_knob_rho(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N, int K,
-                     double *rho, void *stream) {
-    k_knob_rho<<<2, 1024, 0, static_cast<cudaStream_t>(stream)>>>(er, ssr, M, ec, ssc, N, K, rho);
+void launch_knob_stats(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N,
+                       const double *ca, const double *rb, int K, double *out, void *stream) {
+    k_knob_stats<<<3, 1024, 0, static_cast<cudaStream_t>(stream)>>>(er, ssr, M, ec, ssc, N, ca, rb, K, out);
 }
 
 void launch_rowmax(const double *A, long lda, int M, int K, int32_t *er, double *ss, void *stream) {

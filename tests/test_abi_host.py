@@ -1,0 +1,182 @@
+"""CPU tests of the C ABI: the library loads and exports every declared symbol, the
+headers compile, the host-only entry points (planning, precision knob, decode)
+behave, and calls without a GPU fail with status codes instead of crashing.
+"""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import HAVE_GPU, ROOT
+
+INCLUDE = os.path.join(ROOT, "include")
+
+
+def declared_functions():
+    names = set()
+    for h in os.listdir(INCLUDE):
+        if h.endswith(".h") and h != "oz_aie.h":
+            text = open(os.path.join(INCLUDE, h)).read()
+            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+            names |= set(re.findall(r"\b(ozgb_[a-z0-9_]+)\s*\(", text))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol(ozlib):
+    from ozaie_gb300 import _lib
+    lib = ctypes.CDLL(_lib.lib_path())
+    names = declared_functions()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    bound = {n for n, _, _ in _lib.SIGNATURES}
+    assert set(names) <= bound, set(names) - bound
+
+
+def test_c_header_compiles_as_c99_and_cpp(tmp_path):
+    src = tmp_path / "t.c"
+    src.write_text('#include "oz_gb300.h"\nint main(void) { ozgb_handle h = 0; (void)h; return 0; }\n')
+    subprocess.check_call(["gcc", "-std=c99", "-Wall", "-Werror", "-fsyntax-only", "-I", INCLUDE, str(src)])
+    cpp = tmp_path / "t.cpp"
+    cpp.write_text('#include "oz_aie.h"\n#include "oz_aie.h"\nint main() { return oz_aie::Mode::fast; }\n')
+    subprocess.check_call(["g++", "-std=c++17", "-Wall", "-Werror", "-fsyntax-only", "-I", INCLUDE, str(cpp)])
+
+
+def test_dropin_example_builds_and_runs(ozlib, tmp_path):
+    """example/oztest.cpp, the reference's usage, against the drop-in header: it
+    links, and without a GPU it stops at setup with status 2."""
+    from ozaie_gb300 import _lib
+    exe = tmp_path / "oztest"
+    libdir = os.path.dirname(_lib.lib_path())
+    subprocess.check_call(["g++", "-std=c++17", "-I", INCLUDE, os.path.join(ROOT, "example", "oztest.cpp"),
+                           "-L", libdir, "-loz_gb300", "-Wl,-rpath," + libdir, "-o", str(exe)])
+    rc = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert rc.returncode == (0 if HAVE_GPU else 2), rc.stderr
+
+
+@pytest.mark.skipif(HAVE_GPU, reason="checks the no-device path")
+def test_no_device_status_codes(ozlib):
+    h = ozlib.Handle()
+    assert h.setup(256, 512, 128, 0) == 2
+    assert "device" in h.last_error().lower()
+    C = np.zeros((4, 4))
+    assert h.dgemm(4, 4, 4, np.ones((4, 4)), np.ones((4, 4)), C) != 0
+    L = ozlib.load()
+    assert L.ozgb_dgemm_device(h.raw, 4, 4, 4, None, 4, None, 4, None, 4, None) != 0
+    h.close()
+
+
+def test_option_validation(ozlib):
+    L = ozlib.load()
+    h = ozlib.Handle()
+    assert L.ozgb_set_slices(h.raw, 41) == 7 and L.ozgb_set_slices(h.raw, 9) == 0
+    assert L.ozgb_set_bits(h.raw, 8) == 7 and L.ozgb_set_bits(h.raw, 7) == 0
+    assert L.ozgb_set_bins(h.raw, -2) == 7 and L.ozgb_set_bins(h.raw, -1) == 0
+    assert L.ozgb_set_rounding(h.raw, 2) == 7 and L.ozgb_set_rounding(h.raw, 1) == 0
+    assert L.ozgb_set_error_bound(h.raw, -1.0) == 7 and L.ozgb_set_error_bound(h.raw, 1e-15) == 0
+    assert L.ozgb_set_profile(h.raw, 2) == 7 and L.ozgb_set_profile(h.raw, 1) == 0
+    assert L.ozgb_set_timeout_ms(h.raw, 0.0) == 7
+    assert L.ozgb_set_slices(None, 8) == 7
+    h.close()
+
+
+def _pairs(s, J):
+    return sum(1 for p in range(s) for q in range(s) if p + q < J)
+
+
+@pytest.mark.parametrize("shape", [(4096, 4096, 4096), (256, 512, 128), (1, 1, 1), (8192, 8192, 65536),
+                                   (77, 91, 513), (2048, 32, 4096)])
+@pytest.mark.parametrize("b,s,J", [(7, 8, 8), (7, 9, 9), (7, 8, 15), (3, 29, 29), (5, 11, 11), (7, 6, 6)])
+def test_plan_invariants(ozlib, shape, b, s, J):
+    """Every plan covers the bins with contiguous blocks of at most 256 TMEM
+    columns, keeps each fp32 partial sum exact between drains, and has
+    accumulator words for the largest exact sum."""
+    M, N, K = shape
+    c = ozlib.plan_query(M, N, K, b, s, J)
+    assert c is not None
+    assert (c["bits"], c["slices"], c["bins"]) == (b, s, J)
+    assert c["pairs"] == _pairs(s, J)
+    assert c["tile_n"] in (128, 64, 48, 32, 16)
+    lo, nb = c["block_lo"], c["block_nb"]
+    assert lo[0] == 0 and sum(nb) == J
+    assert all(lo[g + 1] == lo[g] + nb[g] for g in range(len(lo) - 1))
+    assert all(n * c["tile_n"] <= 256 for n in nb)
+    max_pairs = max(_pairs(s, j + 1) - _pairs(s, j) for j in range(J))
+    assert max_pairs * c["k_chunk"] * c["drain_chunks"] * (2 ** b - 1) ** 2 <= 2 ** 24
+    qmax = sum((_pairs(s, j + 1) - _pairs(s, j)) * K * (2 ** b - 1) ** 2 << (b * (J - 1 - j)) for j in range(J))
+    assert qmax.bit_length() + 1 <= 32 * c["acc_words"]
+
+
+def test_plan_rejects_inexact_requests(ozlib):
+    assert ozlib.plan_query(128, 128, 128, 7, 30, 59) is None  # more than 8 bin blocks of TMEM
+    assert ozlib.plan_query(0, 128, 128, 7, 8, 8) is None
+
+
+def _stats(A, B):
+    f = lambda x: ((x.view(np.uint64) >> np.uint64(52)) & np.uint64(0x7FF)).astype(np.int32)
+    return (f(A).max(axis=1), (A * A).sum(axis=1), f(B).max(axis=0), (B * B).sum(axis=0), (A * A).sum(axis=0),
+            (B * B).sum(axis=1))
+
+
+def test_precision_knob_estimate_formula(ozlib, oracle):
+    """The knob's estimate against a direct evaluation of its model:
+    est(s) = 1.5 2^-bs ((s-1)/4 sqrt(K SA SB) + sqrt(SA |B|^2 / 3) + sqrt(SB |A|^2 / 3)) / sqrt(T) + 2^-53
+    with SA = sum_i 4^(Er_i-1022), SB likewise, T = sum_k |A(:,k)|^2 |B(k,:)|^2."""
+    K = 200
+    A = oracle.gen_phi((64, K), 1, 1.0)
+    B = oracle.gen_phi((K, 48), 2, 1.0)
+    er, ssr, ec, ssc, ca, rb = _stats(A, B)
+    SA = sum(4.0 ** (int(e) - 1022) for e in er)
+    SB = sum(4.0 ** (int(e) - 1022) for e in ec)
+    T = float(np.sum(ca * rb))
+    nA, nB = float(ssr.sum()), float(ssc.sum())
+
+    def model(t):
+        return 1.5 * 2.0 ** (-7 * t) * ((t - 1) / 4 * (K * SA * SB) ** 0.5 + (SA * nB / 3) ** 0.5 +
+                                        (SB * nA / 3) ** 0.5) / T ** 0.5 + 2.0 ** -53
+
+    for bound in (1e-8, 1e-11, 1e-13, 1e-15):
+        s, est = ozlib.choose_slices(er, ssr, ec, ssc, K, 7, bound, ca, rb)
+        assert est == pytest.approx(model(s), rel=1e-9)
+        assert est <= bound and (s == 2 or model(s - 1) > bound)
+    # without the k-direction sums the mass is taken as spread evenly over k
+    s, est = ozlib.choose_slices(er, ssr, ec, ssc, K, 7, 1e-15)
+    assert 2 <= s <= 16 and est > 0
+
+
+def test_precision_knob_degenerate_statistics(ozlib):
+    """Zero, infinite or NaN statistics give the largest slice count, not a guess."""
+    er = np.full(4, 1023, np.int32)
+    ec = np.full(3, 1023, np.int32)
+    for ss, ka in ((np.ones(4), np.zeros(8)), (np.full(4, np.inf), np.ones(8)), (np.full(4, np.nan), np.ones(8))):
+        s, _ = ozlib.choose_slices(er, ss, ec, np.ones(3), 8, 7, 1e-15, ka, np.ones(8))
+        assert s == 16
+
+
+@pytest.mark.parametrize("phi", [0.1, 0.5, 1.0, 2.0, 4.0])
+def test_precision_knob_meets_bound(ozlib, oracle, phi):
+    """The slice count the knob picks from the stage-(a) statistics meets the
+    requested normwise bound on the exact product (triangular pair set, RN)."""
+    for (M, N, K), seed in (((96, 80, 300), 11), ((64, 64, 2048), 21)):
+        A = oracle.gen_phi((M, K), seed, phi)
+        B = oracle.gen_phi((K, N), seed + 1, phi)
+        er, ssr, ec, ssc, ca, rb = _stats(A, B)
+        rows = np.repeat(np.arange(M, dtype=np.int32), N)
+        cols = np.tile(np.arange(N, dtype=np.int32), M)
+        exact = oracle.exact_entries(A, B, rows, cols)[0].reshape(M, N)
+        last = 0
+        for bound in (1e-8, 1e-11, 1e-13, 1e-15):
+            s, _ = ozlib.choose_slices(er, ssr, ec, ssc, K, 7, bound, ca, rb)
+            assert s >= last
+            last = s
+            C = oracle.dgemm(A, B, 7, s, s, 0)
+            err = np.linalg.norm(C - exact) / np.linalg.norm(exact)
+            assert err <= bound, (bound, s, err)
+
+
+def test_version_string(ozlib):
+    v = ozlib.load().ozgb_version()
+    assert v and v.decode() if isinstance(v, bytes) else v
