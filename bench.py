@@ -116,6 +116,18 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(x, device="cpu"):
+    """Largest value of x over the ranks of the process group (x itself when
+    there is none): the timing that a whole job reports."""
+    import torch
+    import torch.distributed as dist
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -295,10 +307,7 @@ def main():
     clk = clocks.stop()
     if h.sync():
         raise RuntimeError(h.last_error())
-    if ws > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dev)
     flops = 2.0 * M * N * K
     value = flops * ws / (ms * 1e-3) / 1e12
 

@@ -180,3 +180,32 @@ def test_precision_knob_meets_bound(ozlib, oracle, phi):
 def test_version_string(ozlib):
     v = ozlib.load().ozgb_version()
     assert v and v.decode() if isinstance(v, bytes) else v
+
+
+def test_reference_example_compiles_unchanged(ozlib, tmp_path):
+    """The reference's own example program (example/oztest.cpp of Oz-AIE), where
+    its sources are present, compiles and links against the drop-in header as is."""
+    from oracle import build_oracle
+    src = os.path.join(build_oracle.REFERENCE_ROOT, "example", "oztest.cpp")
+    if not os.path.exists(src):
+        pytest.skip("reference sources absent")
+    from ozaie_gb300 import _lib
+    libdir = os.path.dirname(_lib.lib_path())
+    exe = tmp_path / "ref_oztest"
+    subprocess.check_call(["g++", "-std=c++17", "-I", INCLUDE, src, "-L", libdir, "-loz_gb300",
+                           "-Wl,-rpath," + libdir, "-o", str(exe)])
+    rc = subprocess.run([str(exe)], capture_output=True, timeout=120)
+    assert rc.returncode == (0 if HAVE_GPU else 2)
+
+
+def test_cmake_use_ozaie_helper(ozlib, tmp_path):
+    import shutil
+    if not shutil.which("cmake"):
+        pytest.skip("cmake absent")
+    env = dict(os.environ, OZAIE_CMAKE_INCLUDE=os.path.join(INCLUDE, "CMakeLists.txt"))
+    b = tmp_path / "b"
+    subprocess.check_call(["cmake", "-S", os.path.join(ROOT, "example"), "-B", str(b)], env=env,
+                          stdout=subprocess.DEVNULL)
+    subprocess.check_call(["cmake", "--build", str(b)], env=env, stdout=subprocess.DEVNULL)
+    rc = subprocess.run([str(b / "oztest")], capture_output=True, timeout=120)
+    assert rc.returncode == (0 if HAVE_GPU else 2)
