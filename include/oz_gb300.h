@@ -40,7 +40,8 @@ typedef enum {
     OZGB_ERR_ARG = 7,           /* null pointer or invalid option value */
     OZGB_ERR_ALLOC = 8,         /* device memory allocation failed */
     OZGB_ERR_TIMEOUT = 9,       /* a device-side wait ran out of time; the kernel stopped early */
-    OZGB_ERR_UNSUPPORTED = 10   /* the requested slices/bins exceed the exact-accumulation limits */
+    OZGB_ERR_UNSUPPORTED = 10,  /* the requested slices/bins exceed the exact-accumulation limits */
+    OZGB_ERR_TOO_LARGE = 11     /* ozgb_dgemm_device_noalloc: the problem needs more than its fixed scratch */
 } ozgb_status;
 
 typedef enum { OZGB_MODE_ACCURATE = 0, OZGB_MODE_FAST = 1 } ozgb_mode; /* oz_aie::Mode, include/oz_aie.h:82 */
@@ -98,6 +99,25 @@ ozgb_status ozgb_dgemm_device(ozgb_handle h, int M, int N, int K, const double *
                               const double *dB, long ldb, double *dC, long ldc, void *stream);
 /* Waits for the last enqueued call and checks the device error word. */
 ozgb_status ozgb_sync(ozgb_handle h);
+
+/* ------------------------------------------------- no device allocation */
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc:
+ * code inside another framework's memory pool or caching allocator, code that
+ * must not trigger the device synchronisation of cudaMalloc/cudaFree, code with
+ * a memory budget fixed in advance.  Same product as ozgb_dgemm_device (device
+ * arrays, leading dimensions, enqueued on `stream`, NULL = default stream) with
+ * b = 7, `slices` in [2, 16], triangular pair set, round to nearest; no handle.
+ * All scratch comes from one 64 MiB static device array reserved when the
+ * library loads; a product needs about 4 (M + N) + 2 s (Mp + Np) Kp bytes
+ * (Mp, Np, Kp: M, N, K rounded up to the tile sizes), e.g. 1024^3 up to s = 15,
+ * 2048 x 2048 x 1024 up to s = 7.  Larger products return OZGB_ERR_TOO_LARGE.
+ * The first call on a device (with it current) sets up the array's address:
+ * make that first call before any stream capture.  Calls share the array:
+ * calls that overlap on the GPU race.  Device-side wait timeouts (a stalled
+ * GPU) leave C incomplete and are not reported here; ozgb_dgemm_device with
+ * ozgb_sync reports them. */
+ozgb_status ozgb_dgemm_device_noalloc(int M, int N, int K, const double *dA, long lda, const double *dB, long ldb,
+                                      double *dC, long ldc, int slices, void *stream);
 
 /* --------------------------------------------------------------- grouped */
 typedef struct {

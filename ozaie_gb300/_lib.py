@@ -52,7 +52,7 @@ class OzgbProblem(ctypes.Structure):
 STATUS = {
     0: "OZGB_OK", 1: "OZGB_ERR_DIMS", 2: "OZGB_ERR_NO_DEVICE", 3: "OZGB_ERR_EXEC", 4: "OZGB_ERR_IMAGE",
     5: "OZGB_ERR_NOT_SETUP", 6: "OZGB_ERR_DIM_MISMATCH", 7: "OZGB_ERR_ARG", 8: "OZGB_ERR_ALLOC",
-    9: "OZGB_ERR_TIMEOUT", 10: "OZGB_ERR_UNSUPPORTED",
+    9: "OZGB_ERR_TIMEOUT", 10: "OZGB_ERR_UNSUPPORTED", 11: "OZGB_ERR_TOO_LARGE",
 }
 
 # (name, restype, argtypes) for every function of include/oz_gb300.h
@@ -87,6 +87,7 @@ SIGNATURES = [
     ("ozgb_convert_paired_i64_to_double", _i, [_p, _p, _i, _i, _i, _i, _i]),
     ("ozgb_plan_query", _i, [_i, _i, _i, _i, _i, _i, ctypes.POINTER(OzgbConfig)]),
     ("ozgb_choose_slices", _i, [_p, _p, _i, _p, _p, _i, _p, _p, _i, _i, _dbl, ctypes.POINTER(_dbl)]),
+    ("ozgb_dgemm_device_noalloc", _i, [_i, _i, _i, _p, ctypes.c_long, _p, ctypes.c_long, _p, ctypes.c_long, _i, _p]),
     ("ozgb_launch_count", _i, [_h, ctypes.POINTER(ctypes.c_longlong)]),
     ("ozgb_version", ctypes.c_char_p, []),
 ]

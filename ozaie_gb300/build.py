@@ -21,6 +21,7 @@ SOURCES = [
     "oz_gemm_v4.cu",
     "oz_split.cu",
     "oz_capi.cu",
+    "oz_noalloc.cu",
     "oz_plan.cpp",
 ]
 
