@@ -292,6 +292,23 @@ struct DrainSchedule {
 #endif
 
 // ------------------------------------------------------------------ kernel
+// Grouped rasterisation: 8 M-tiles share the same stream of B tiles.
+__device__ __forceinline__ void tile_coords(const GemmArgs &g, int t, int *mt, int *nt) {
+    const int GM = 8;
+    const int per_group = GM * g.tiles_n;
+    const int grp = t / per_group;
+    const int first_m = grp * GM;
+    const int gm = min(GM, g.tiles_m - first_m);
+    const int r = t - grp * per_group;
+    *mt = first_m + r % gm;
+    *nt = r / gm;
+}
+
+// Persistent: CTA b processes tiles b, b + gridDim.x, ...  The stage ring, the
+// bin-block barriers and TMEM persist across tiles, so the producer prefetches
+// the next tile's first chunks and the UMMAs of the next tile start as soon as
+// each block's final drain of the previous tile has read it out, while the
+// drain warps round and store the previous tile.
 template <int BN, int W, int KC>
 __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_constant__ GemmArgs g) {
     constexpr int PARTS = kEpiWarps / 4;          // drain warps sharing one TMEM lane quadrant
@@ -320,24 +337,11 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
     int *blk_np = reinterpret_cast<int *>(blk_id + kMaxGroups);             // A slices per UMMA run
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n_tiles = g.tiles_m * g.tiles_n;
 #ifdef OZGB_PROBE
     long long pr0 = 0, pr1 = 0, pr2 = 0, pr3 = 0;
     const long long pstart = clock64();
 #endif
-
-    // grouped rasterisation: 8 M-tiles share the same stream of B tiles
-    int mt, nt;
-    {
-        const int GM = 8;
-        const int t = blockIdx.x;
-        const int per_group = GM * g.tiles_n;
-        const int grp = t / per_group;
-        const int first_m = grp * GM;
-        const int gm = min(GM, g.tiles_m - first_m);
-        const int r = t - grp * per_group;
-        mt = first_m + r % gm;
-        nt = r / gm;
-    }
 
     // zero B slices below and above the loaded ones (read by out-of-range pairs)
     {
@@ -378,45 +382,50 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
     if (warp == 0) {
         // ------------------------------------------------------ producer
         if (lane == 0) {
-            const uint8_t *a_src = reinterpret_cast<const uint8_t *>(g.a_tiles) +
-                                   static_cast<size_t>(mt) * g.n_kc * g.a_block_bytes;
-            const uint8_t *b_src = reinterpret_cast<const uint8_t *>(g.b_tiles) +
-                                   static_cast<size_t>(nt) * g.n_kc * g.b_block_bytes;
-            int issued = 0;
+            long long issued = 0;  // chunks issued by this CTA over all of its tiles
             int st = 0;
-            uint32_t eparity = 0;
-            DrainSchedule pds;
-            pds.init(g);
-            for (int c = 0; c < g.n_kc; ++c) {
-                if (*vabort) break;
-                OZ_PT(tw);
-                const bool got = (c < g.stages) || mbar_wait(&empty[st], eparity, vabort, TO);
-                OZ_PADD(pr0, tw);
-                if (!got) {
-                    if (!*vabort) {
-                        atomicCAS(g.err, 0, DEVERR_TIMEOUT_PRODUCER);
-                        *vabort = 1;
+            bool ok = true;
+            for (int t = blockIdx.x; ok && t < n_tiles; t += gridDim.x) {
+                int mt, nt;
+                tile_coords(g, t, &mt, &nt);
+                const uint8_t *a_src = reinterpret_cast<const uint8_t *>(g.a_tiles) +
+                                       static_cast<size_t>(mt) * g.n_kc * g.a_block_bytes;
+                const uint8_t *b_src = reinterpret_cast<const uint8_t *>(g.b_tiles) +
+                                       static_cast<size_t>(nt) * g.n_kc * g.b_block_bytes;
+                DrainSchedule pds;
+                pds.init(g);
+                for (int c = 0; c < g.n_kc; ++c) {
+                    if (*vabort) {
+                        ok = false;
+                        break;
                     }
-                    break;
-                }
-                uint8_t *dst = smem + static_cast<size_t>(st) * g.stage_bytes;
-                stage_mask[st] = pds.next(g, c == g.n_kc - 1);  // published by the arrive below
-                mbar_arrive_expect_tx(&full[st], g.a_block_bytes + g.b_block_bytes);
-                bulk_g2s(dst, a_src + static_cast<size_t>(c) * g.a_block_bytes, g.a_block_bytes, &full[st]);
-                bulk_g2s(dst + g.a_block_bytes + g.b_pad_lo_bytes, b_src + static_cast<size_t>(c) * g.b_block_bytes,
-                         g.b_block_bytes, &full[st]);
-                ++issued;
-                if (++st == g.stages) {
-                    st = 0;
-                    // the wait before reusing stage st in round r (>= 1) is on the
-                    // (r-1)-th completion of empty[st]: parity (r - 1) & 1
-                    if (c + 1 > g.stages) eparity ^= 1u;
+                    // use r of stage st (r >= 1) waits for the (r-1)-th release of that stage
+                    const long long r = issued / g.stages;
+                    OZ_PT(tw);
+                    const bool got = (r == 0) || mbar_wait(&empty[st], static_cast<uint32_t>((r - 1) & 1), vabort, TO);
+                    OZ_PADD(pr0, tw);
+                    if (!got) {
+                        if (!*vabort) {
+                            atomicCAS(g.err, 0, DEVERR_TIMEOUT_PRODUCER);
+                            *vabort = 1;
+                        }
+                        ok = false;
+                        break;
+                    }
+                    uint8_t *dst = smem + static_cast<size_t>(st) * g.stage_bytes;
+                    stage_mask[st] = pds.next(g, c == g.n_kc - 1);  // published by the arrive below
+                    mbar_arrive_expect_tx(&full[st], g.a_block_bytes + g.b_block_bytes);
+                    bulk_g2s(dst, a_src + static_cast<size_t>(c) * g.a_block_bytes, g.a_block_bytes, &full[st]);
+                    bulk_g2s(dst + g.a_block_bytes + g.b_pad_lo_bytes,
+                             b_src + static_cast<size_t>(c) * g.b_block_bytes, g.b_block_bytes, &full[st]);
+                    ++issued;
+                    if (++st == g.stages) st = 0;
                 }
             }
             // every copy issued must land before the CTA may exit
             const int zero = 0;
-            for (int c = (issued > g.stages ? issued - g.stages : 0); c < issued; ++c)
-                mbar_wait(&full[c % g.stages], (c / g.stages) & 1, &zero, TO);
+            for (long long c = (issued > g.stages ? issued - g.stages : 0); c < issued; ++c)
+                mbar_wait(&full[c % g.stages], static_cast<uint32_t>((c / g.stages) & 1), &zero, TO);
         }
     } else if (warp == 1) {
         // ---------------------------------------------------- MMA issuer
@@ -445,72 +454,77 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
             }
             const uint32_t all = (1u << g.G) - 1u;
             uint64_t ephase = 0;            // per-block parity of gempty waits
-            uint32_t prev = 0;              // blocks drained after the previous chunk
+            uint32_t prev = 0;              // blocks drained after the previous chunk (of any tile)
             uint32_t fresh = all;           // blocks whose next UMMA overwrites the accumulators
             int st = 0;
             uint32_t fparity = 0;
             bool ok = true;
-            for (int c = 0; ok && c < g.n_kc; ++c) {
-                OZ_PT(tf);
-                const bool gotf = mbar_wait(&full[st], fparity, vabort, TO);
-                OZ_PADD(pr0, tf);
-                if (!gotf) { ok = false; break; }
-                tc_fence_after();
-                OZ_PT(ti);
-                const uint64_t stage_off = (static_cast<uint64_t>(st) * g.stage_bytes) >> 4;
-                const uint32_t cur = stage_mask[st];
-                // issue order: blocks drained after this chunk, then the rest, then the
-                // blocks whose drain (after the previous chunk) must finish first
-                uint32_t order[3] = {cur & ~prev, all & ~cur & ~prev, prev};
-                for (int cls = 0; ok && cls < 3; ++cls) {
-                    uint32_t m = order[cls];
-                    while (m) {
-                        const int blk = __ffs(m) - 1;
-                        const uint32_t bit = 1u << blk;
-                        m &= m - 1;
-                        if (cls == 2) {
-                            OZ_PT(te);
-                            const bool gote = mbar_wait(&gempty[blk], static_cast<uint32_t>((ephase >> blk) & 1ull),
-                                                        vabort, TO);
-                            OZ_PADD(pr1, te);
-                            if (!gote) {
-                                ok = false;
-                                break;
+            for (int t = blockIdx.x; ok && t < n_tiles; t += gridDim.x) {
+                for (int c = 0; ok && c < g.n_kc; ++c) {
+                    OZ_PT(tf);
+                    const bool gotf = mbar_wait(&full[st], fparity, vabort, TO);
+                    OZ_PADD(pr0, tf);
+                    if (!gotf) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    OZ_PT(ti);
+                    const uint64_t stage_off = (static_cast<uint64_t>(st) * g.stage_bytes) >> 4;
+                    const uint32_t cur = stage_mask[st];
+                    // issue order: blocks drained after this chunk, then the rest, then the
+                    // blocks whose drain (after the previous chunk) must finish first
+                    uint32_t order[3] = {cur & ~prev, all & ~cur & ~prev, prev};
+                    for (int cls = 0; ok && cls < 3; ++cls) {
+                        uint32_t m = order[cls];
+                        while (m) {
+                            const int blk = __ffs(m) - 1;
+                            const uint32_t bit = 1u << blk;
+                            m &= m - 1;
+                            if (cls == 2) {
+                                OZ_PT(te);
+                                const bool gote = mbar_wait(&gempty[blk],
+                                                            static_cast<uint32_t>((ephase >> blk) & 1ull), vabort, TO);
+                                OZ_PADD(pr1, te);
+                                if (!gote) {
+                                    ok = false;
+                                    break;
+                                }
+                                ephase ^= (1ull << blk);
+                                tc_fence_after();
                             }
-                            ephase ^= (1ull << blk);
-                            tc_fence_after();
-                        }
-                        const uint32_t d_tmem = blk_tm[blk];
-                        const uint32_t idesc = blk_id[blk];
-                        const int np = blk_np[blk];
-                        uint64_t ad = blk_ad[blk] + stage_off;
-                        uint64_t bd = blk_bd[blk] + stage_off;
-                        uint32_t acc = (fresh & bit) ? 0u : 1u;
-                        for (int p = 0; p < np; ++p) {
+                            const uint32_t d_tmem = blk_tm[blk];
+                            const uint32_t idesc = blk_id[blk];
+                            const int np = blk_np[blk];
+                            uint64_t ad = blk_ad[blk] + stage_off;
+                            uint64_t bd = blk_bd[blk] + stage_off;
+                            uint32_t acc = (fresh & bit) ? 0u : 1u;
+                            for (int p = 0; p < np; ++p) {
 #pragma unroll
-                            for (int kk = 0; kk < ksteps; ++kk) {
-                                umma_bf16(d_tmem, ad + static_cast<uint64_t>(kk * 16), bd + static_cast<uint64_t>(kk * 16),
-                                          idesc, acc);
-                                acc = 1u;
+                                for (int kk = 0; kk < ksteps; ++kk) {
+                                    umma_bf16(d_tmem, ad + static_cast<uint64_t>(kk * 16),
+                                              bd + static_cast<uint64_t>(kk * 16), idesc, acc);
+                                    acc = 1u;
+                                }
+                                ad += a_step;
+                                bd -= b_step;
                             }
-                            ad += a_step;
-                            bd -= b_step;
-                        }
-                        fresh &= ~bit;
-                        if (cur & bit) {
-                            umma_commit(&gfull[blk]);
-                            fresh |= bit;
+                            fresh &= ~bit;
+                            if (cur & bit) {
+                                umma_commit(&gfull[blk]);
+                                fresh |= bit;
+                            }
                         }
                     }
+                    OZ_PADD(pr2, ti);
+                    if (!ok) break;
+                    umma_commit(&empty[st]);
+                    if (++st == g.stages) {
+                        st = 0;
+                        fparity ^= 1u;
+                    }
+                    prev = cur;
                 }
-                OZ_PADD(pr2, ti);
-                if (!ok) break;
-                umma_commit(&empty[st]);
-                if (++st == g.stages) {
-                    st = 0;
-                    fparity ^= 1u;
-                }
-                prev = cur;
             }
             if (!ok && !*vabort) {
                 atomicCAS(g.err, 0, DEVERR_TIMEOUT_MMA);
@@ -530,72 +544,71 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
         const uint32_t trow = tmem + (static_cast<uint32_t>(32 * qd) << 16) + static_cast<uint32_t>(part * COLS);
 
         uint32_t q[COLS][W];
-#pragma unroll
-        for (int i = 0; i < COLS; ++i)
-#pragma unroll
-            for (int w = 0; w < W; ++w) q[i][w] = 0;
-
-        DrainSchedule ds;
-        ds.init(g);
         uint64_t fphase = 0;
         uint32_t prev = 0;
         bool ok = true;
-        for (int c = 0; ok && c < g.n_kc; ++c) {
-            const bool last = (c == g.n_kc - 1);
-            const uint32_t cur = ds.next(g, last);
-            for (int pass = 0; ok && pass < 2; ++pass) {
-                uint32_t m = pass == 0 ? (cur & ~prev) : (cur & prev);
-                while (m) {
-                    const int blk = __ffs(m) - 1;
-                    m &= m - 1;
-                    OZ_PT(tg);
-                    const bool gotg = mbar_wait(&gfull[blk], static_cast<uint32_t>((fphase >> blk) & 1ull), vabort, TO);
-                    OZ_PADD(pr0, tg);
-                    if (!gotg) {
-                        ok = false;
-                        break;
-                    }
-                    fphase ^= (1ull << blk);
-                    tc_fence_after();
-                    OZ_PT(td);
-                    int lo = 0, nb = 0;  // static-index selects (see the MMA issuer)
+        for (int t = blockIdx.x; ok && t < n_tiles; t += gridDim.x) {
+            int mt, nt;
+            tile_coords(g, t, &mt, &nt);
 #pragma unroll
-                    for (int i = 0; i < kMaxGroups; ++i)
-                        if (i == blk) {
-                            lo = g.blk_lo[i];
-                            nb = g.blk_nb[i];
+            for (int i = 0; i < COLS; ++i)
+#pragma unroll
+                for (int w = 0; w < W; ++w) q[i][w] = 0;
+
+            DrainSchedule ds;
+            ds.init(g);
+            for (int c = 0; ok && c < g.n_kc; ++c) {
+                const bool last = (c == g.n_kc - 1);
+                const uint32_t cur = ds.next(g, last);
+                for (int pass = 0; ok && pass < 2; ++pass) {
+                    uint32_t m = pass == 0 ? (cur & ~prev) : (cur & prev);
+                    while (m) {
+                        const int blk = __ffs(m) - 1;
+                        m &= m - 1;
+                        OZ_PT(tg);
+                        const bool gotg =
+                            mbar_wait(&gfull[blk], static_cast<uint32_t>((fphase >> blk) & 1ull), vabort, TO);
+                        OZ_PADD(pr0, tg);
+                        if (!gotg) {
+                            ok = false;
+                            break;
                         }
-                    const int hi = lo + nb - 1;
-                    for (int j = lo; j <= hi; ++j) {
-                        const int sh = g.b * (g.J - 1 - j);
+                        fphase ^= (1ull << blk);
+                        tc_fence_after();
+                        OZ_PT(td);
+                        int lo = 0, nb = 0;  // static-index selects (see the MMA issuer)
 #pragma unroll
-                        for (int cb = 0; cb < COLS / DB; ++cb) {
-                            uint32_t v[DB];
-                            tmem_ld_cols<DB>(trow + j * BN + cb * DB, v);
-                            tmem_ld_wait();
+                        for (int i = 0; i < kMaxGroups; ++i)
+                            if (i == blk) {
+                                lo = g.blk_lo[i];
+                                nb = g.blk_nb[i];
+                            }
+                        const int hi = lo + nb - 1;
+                        for (int j = lo; j <= hi; ++j) {
+                            const int sh = g.b * (g.J - 1 - j);
 #pragma unroll
-                            for (int i = 0; i < DB; ++i) reg_fence(v[i]);
-                            q_add_shifted<W, DB>(q + cb * DB, v, sh);
+                            for (int cb = 0; cb < COLS / DB; ++cb) {
+                                uint32_t v[DB];
+                                tmem_ld_cols<DB>(trow + j * BN + cb * DB, v);
+                                tmem_ld_wait();
+#pragma unroll
+                                for (int i = 0; i < DB; ++i) reg_fence(v[i]);
+                                q_add_shifted<W, DB>(q + cb * DB, v, sh);
+                            }
                         }
-                    }
-                    if (!last) {
+                        // the block's accumulators are free for the next chunk (or tile)
                         tc_fence_before();
                         __syncwarp();
                         if (lane == 0) mbar_arrive(&gempty[blk]);
+                        OZ_PADD(pr1, td);
                     }
-                    OZ_PADD(pr1, td);
                 }
+                prev = cur;
             }
-            prev = cur;
-        }
-        if (!ok && !*vabort) {
-            atomicCAS(g.err, 0, DEVERR_TIMEOUT_EPI);
-            *vabort = 1;
-        }
+            if (!ok) break;
 
-        // ------------------------------------------------------- epilogue
-        OZ_PT(tq);
-        if (ok) {
+            // --------------------------------------------------- epilogue
+            OZ_PT(tq);
             const int row = mt * BM + 32 * qd + lane;
             const int col0 = nt * BN + part * COLS;
             if (row < g.M) {
@@ -621,8 +634,12 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                     }
                 }
             }
+            OZ_PADD(pr2, tq);
         }
-        OZ_PADD(pr2, tq);
+        if (!ok && !*vabort) {
+            atomicCAS(g.err, 0, DEVERR_TIMEOUT_EPI);
+            *vabort = 1;
+        }
     }
 
     __syncthreads();
@@ -641,10 +658,24 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
     }
 }
 
+// Number of SMs of the current device (one persistent CTA each).
+inline int device_sm_count() {
+    static int cached[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
+    if (!cached[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 148;
+        cached[dev] = n;
+    }
+    return cached[dev];
+}
+
 template <int BN, int W, int KC>
-void launch_gemm_variant(const GemmArgs &args, int grid, size_t smem, void *stream) {
+void launch_gemm_variant(const GemmArgs &args, int tiles, size_t smem, void *stream) {
     auto kern = oz_gemm_kernel<BN, W, KC>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    const int grid = tiles < device_sm_count() ? tiles : device_sm_count();
     kern<<<grid, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(args);
 }
 
