@@ -280,7 +280,7 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
         for (size_t i = 0; i < need; ++i) sum[i % 8] += static_cast<double>(hp[i]);
         const double n = static_cast<double>(need / 8);
         fprintf(stderr,
-                "OZGB_PROBE ctas=%.0f avg cycles per CTA: producer_wait=%.0f mma_wait_full=%.0f "
+                "OZGB_PROBE tiles=%.0f cycles per tile (CTA sums / tiles): producer_wait=%.0f mma_wait_full=%.0f "
                 "mma_wait_drained=%.0f mma_issue=%.0f drain_wait=%.0f drain_work=%.0f epilogue=%.0f total=%.0f "
                 "(n_kc=%d blocks=%d)\n",
                 n, sum[0] / n, sum[1] / n, sum[2] / n, sum[3] / n, sum[4] / n, sum[5] / n, sum[6] / n, sum[7] / n,

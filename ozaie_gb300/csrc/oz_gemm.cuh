@@ -7,7 +7,8 @@
 //   bin-weighted sum + exponent scale-back         src/aie_kernels/generic/ozaki_base.cc:143-340
 //   int128 -> double reconstruction                include/oz_aie.h:92-150
 //
-// GB300 design (one CTA per 128 x BN tile of C, 320 threads):
+// GB300 design (persistent CTAs, one per SM, each looping over 128 x BN tiles of
+// C; 576 threads: producer warp, MMA-issuer warp, 16 drain/epilogue warps):
 //   * Carrier: tcgen05.mma kind::f16 with bf16 slices (|v| <= 127 is exact in
 //     bf16) and fp32 accumulators in TMEM.  (kind::i8 is not accepted by ptxas
 //     for sm_103a.)  Every partial sum is an integer of magnitude <= 2^24 as
@@ -29,7 +30,7 @@
 //     chunk (after waiting for their drain): a drain overlaps the UMMAs of the
 //     other blocks.  The first UMMA of a block after a drain overwrites the
 //     accumulators (enable_input_d = 0), so TMEM is never cleared explicitly.
-//   * Drain (warps 2..9): TMEM -> registers, fp32 -> int32 (exact), shifted by
+//   * Drain (warps 2..17): TMEM -> registers, fp32 -> int32 (exact), shifted by
 //     b(J-1-j) and added into a W-word two's complement accumulator per element.
 //   * Epilogue: the exact accumulator q is rounded once to FP64 with the scale
 //     2^{Er+Ec-2044-b(J+1)} (round-to-nearest, or the reference's truncating
