@@ -67,7 +67,14 @@ struct ozgb_context {
     bool have_last = false;
     // buffers
     DevBuf a, b, c, at, bt, er, ec, ssr, ssc, err, raw, knob, kca, krb, ktmp;
+    DevBuf gstat, gslice, gtab;  // grouped calls: statistics, slice planes, job/problem tables
     cudaStream_t stream = nullptr;       // used by the host-array entry points
+    // grouped calls: the per-problem GEMMs run on auxiliary streams forked from
+    // and joined back into the caller's stream
+    static constexpr int kAux = 8;
+    cudaStream_t aux[kAux] = {};
+    cudaEvent_t ev_fork = nullptr;
+    cudaEvent_t ev_join[kAux] = {};
     cudaStream_t last_stream = nullptr;  // stream of the last enqueued call
     // profiling
     bool profiling = false;
@@ -206,6 +213,35 @@ ozgb_status choose_config(ozgb_handle h, const Operands &o, int mode, cudaStream
     return OZGB_OK;
 }
 
+// GEMM launch arguments that follow from the plan alone (shared by all problems
+// of a grouped launch); operands, sizes and tiles are set by the caller.
+void gemm_args_from_plan(GemmArgs *g, const Plan &p, int out_mode, int *err, unsigned long long timeout_ns) {
+    memset(g, 0, sizeof *g);
+    g->KC = p.KC;
+    g->s = p.cfg.s;
+    g->J = p.cfg.J;
+    g->b = p.cfg.b;
+    g->out_mode = out_mode;
+    g->stages = p.stages;
+    g->stage_bytes = p.stage_bytes;
+    g->a_block_bytes = p.a_block_bytes;
+    g->b_block_bytes = p.b_block_bytes;
+    g->b_pad_lo_bytes = static_cast<uint32_t>(p.pad_lo) * p.b_slice_bytes;
+    g->b_region_bytes = p.b_region_bytes;
+    g->tmem_cols = p.tmem_cols;
+    g->err = err;
+    g->timeout_ns = timeout_ns;
+    g->G = p.G;
+    for (int i = 0; i < p.G; ++i) {
+        g->blk_lo[i] = p.blk_lo[i];
+        g->blk_nb[i] = p.blk_nb[i];
+        g->blk_p0[i] = p.blk_p0[i];
+        g->blk_p1[i] = p.blk_p1[i];
+        g->blk_period[i] = p.blk_period[i];
+        g->blk_off[i] = p.blk_off[i];
+    }
+}
+
 // Stages (b) and (c)+(d) for one problem whose exponents are in h->er / h->ec.
 ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, int out_mode, int32_t *raw,
                                cudaStream_t st) {
@@ -218,7 +254,7 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
     h->launches += 2;
     if (h->profiling) cudaEventRecord(h->ev[2], st);
     GemmArgs g;
-    memset(&g, 0, sizeof g);
+    gemm_args_from_plan(&g, p, out_mode, static_cast<int *>(h->err.p), h->timeout_ns);
     g.a_tiles = at;
     g.b_tiles = bt;
     g.er = static_cast<int32_t *>(h->er.p);
@@ -229,31 +265,9 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
     g.M = o.M;
     g.N = o.N;
     g.n_kc = p.n_kc;
-    g.KC = p.KC;
-    g.s = p.cfg.s;
-    g.J = p.cfg.J;
-    g.b = p.cfg.b;
-    g.out_mode = out_mode;
     g.tiles_m = p.tiles_m;
     g.tiles_n = p.tiles_n;
-    g.stages = p.stages;
-    g.stage_bytes = p.stage_bytes;
-    g.a_block_bytes = p.a_block_bytes;
-    g.b_block_bytes = p.b_block_bytes;
-    g.b_pad_lo_bytes = static_cast<uint32_t>(p.pad_lo) * p.b_slice_bytes;
-    g.b_region_bytes = p.b_region_bytes;
-    g.tmem_cols = p.tmem_cols;
-    g.err = static_cast<int *>(h->err.p);
-    g.timeout_ns = h->timeout_ns;
-    g.G = p.G;
-    for (int i = 0; i < p.G; ++i) {
-        g.blk_lo[i] = p.blk_lo[i];
-        g.blk_nb[i] = p.blk_nb[i];
-        g.blk_p0[i] = p.blk_p0[i];
-        g.blk_p1[i] = p.blk_p1[i];
-        g.blk_period[i] = p.blk_period[i];
-        g.blk_off[i] = p.blk_off[i];
-    }
+    g.total_tiles = p.tiles_m * p.tiles_n;
 #ifdef OZGB_PROBE
     // probe builds: per-CTA cycle counters of the GEMM roles, summarised on stderr
     static unsigned long long *probe = nullptr;
@@ -329,6 +343,255 @@ ozgb_status check_device_error(ozgb_handle h, cudaStream_t st) {
     return OZGB_OK;
 }
 
+// ------------------------------------------------------------ grouped calls
+size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
+
+// Plan fields that the GEMM kernel takes from its launch arguments: problems
+// whose plans agree on all of them share one grouped launch.
+bool same_launch_class(const Plan &x, const Plan &y) {
+    if (x.fn != y.fn || x.cfg.b != y.cfg.b || x.cfg.s != y.cfg.s || x.cfg.J != y.cfg.J ||
+        x.cfg.rounding != y.cfg.rounding || x.KC != y.KC || x.stages != y.stages || x.stage_bytes != y.stage_bytes ||
+        x.a_block_bytes != y.a_block_bytes || x.b_block_bytes != y.b_block_bytes || x.pad_lo != y.pad_lo ||
+        x.b_region_bytes != y.b_region_bytes || x.tmem_cols != y.tmem_cols || x.smem != y.smem || x.G != y.G)
+        return false;
+    for (int i = 0; i < x.G; ++i)
+        if (x.blk_lo[i] != y.blk_lo[i] || x.blk_nb[i] != y.blk_nb[i] || x.blk_p0[i] != y.blk_p0[i] ||
+            x.blk_p1[i] != y.blk_p1[i] || x.blk_period[i] != y.blk_period[i] || x.blk_off[i] != y.blk_off[i])
+            return false;
+    return true;
+}
+
+// Uploads a host table into the grouped-table buffer at byte offset *off.
+template <typename T>
+const T *put_table(ozgb_handle h, const std::vector<T> &v, size_t *off, cudaStream_t st) {
+    uint8_t *dst = static_cast<uint8_t *>(h->gtab.p) + *off;
+    cudaMemcpyAsync(dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st);
+    *off += align256(sizeof(T) * v.size());
+    return reinterpret_cast<const T *>(dst);
+}
+
+// All stage jobs of one grouped launch, with their block offsets.
+struct JobList {
+    std::vector<StageJob> jobs;
+    std::vector<int> block0;
+    int total = 0;
+    void add(const StageJob &j0) {
+        StageJob j = j0;
+        stage_grid(j, &j.gx, &j.gy);
+        block0.push_back(total);
+        total += j.gx * j.gy;
+        jobs.push_back(j);
+    }
+};
+
+// The grouped pipeline: one launch for every problem's stage (a) (and the knob's
+// statistics), one grouped knob reduction and a single read-back when any
+// problem asks for an error bound, one launch for every problem's split, and one
+// persistent slice-pair GEMM launch per class of problems sharing a plan.
+ozgb_status enqueue_grouped(ozgb_handle h, ozgb_problem *probs, int n, int mode, cudaStream_t st) {
+    std::vector<double> bound(n, 0.0);
+    int n_adapt = 0;
+    for (int i = 0; i < n; ++i) {
+        double bd = probs[i].error_bound;
+        if (!(bd > 0.0) && h->err_bound > 0.0 && h->opt_slices <= 0) bd = h->err_bound;
+        bound[i] = bd > 0.0 ? bd : 0.0;
+        if (bound[i] > 0.0) ++n_adapt;
+    }
+    // ---- statistics scratch: er, ec (int32); ssr, ssc, ca, rb (double) when adaptive
+    struct StatOff {
+        size_t er, ec, ssr, ssc, ca, rb, out;
+    };
+    std::vector<StatOff> so(n);
+    size_t total = 0;
+    for (int i = 0; i < n; ++i) {
+        const ozgb_problem &pb = probs[i];
+        so[i].er = total;
+        total += align256(sizeof(int32_t) * pb.M);
+        so[i].ec = total;
+        total += align256(sizeof(int32_t) * pb.N);
+        if (bound[i] > 0.0) {
+            so[i].ssr = total;
+            total += align256(sizeof(double) * pb.M);
+            so[i].ssc = total;
+            total += align256(sizeof(double) * pb.N);
+            so[i].ca = total;
+            total += align256(sizeof(double) * pb.K);
+            so[i].rb = total;
+            total += align256(sizeof(double) * pb.K);
+            so[i].out = total;
+            total += 256;
+        }
+    }
+    if (!h->gstat.ensure(total)) return fail(h, OZGB_ERR_ALLOC, "grouped statistics buffer");
+    uint8_t *gs = static_cast<uint8_t *>(h->gstat.p);
+    auto at = [&](size_t off) { return gs + off; };
+
+    // ---- stage (a) jobs
+    JobList ja;
+    for (int i = 0; i < n; ++i) {
+        const ozgb_problem &pb = probs[i];
+        const bool ad = bound[i] > 0.0;
+        StageJob j{};
+        j.kind = JOB_ROWMAX, j.X = pb.A, j.ld = pb.lda, j.rows = pb.M, j.cols = pb.K;
+        j.e_out = reinterpret_cast<int32_t *>(at(so[i].er));
+        j.ss_out = ad ? reinterpret_cast<double *>(at(so[i].ssr)) : nullptr;
+        ja.add(j);
+        j = StageJob{};
+        j.kind = JOB_COLMAX, j.X = pb.B, j.ld = pb.ldb, j.rows = pb.K, j.cols = pb.N;
+        j.e_out = reinterpret_cast<int32_t *>(at(so[i].ec));
+        j.ss_out = ad ? reinterpret_cast<double *>(at(so[i].ssc)) : nullptr;
+        ja.add(j);
+        if (ad) {
+            j = StageJob{};
+            j.kind = JOB_COLMAX, j.X = pb.A, j.ld = pb.lda, j.rows = pb.M, j.cols = pb.K;
+            j.ss_out = reinterpret_cast<double *>(at(so[i].ca));
+            ja.add(j);
+            j = StageJob{};
+            j.kind = JOB_ROWMAX, j.X = pb.B, j.ld = pb.ldb, j.rows = pb.K, j.cols = pb.N;
+            j.ss_out = reinterpret_cast<double *>(at(so[i].rb));
+            ja.add(j);
+        }
+    }
+    ja.block0.push_back(ja.total);
+    std::vector<KnobJob> kj;
+    for (int i = 0; i < n; ++i)
+        if (bound[i] > 0.0)
+            kj.push_back(KnobJob{reinterpret_cast<int32_t *>(at(so[i].er)), reinterpret_cast<double *>(at(so[i].ssr)),
+                                 probs[i].M, reinterpret_cast<int32_t *>(at(so[i].ec)),
+                                 reinterpret_cast<double *>(at(so[i].ssc)), probs[i].N,
+                                 reinterpret_cast<double *>(at(so[i].ca)), reinterpret_cast<double *>(at(so[i].rb)),
+                                 probs[i].K, reinterpret_cast<double *>(at(so[i].out))});
+    size_t tab_bytes = align256(sizeof(StageJob) * ja.jobs.size()) + align256(sizeof(int) * ja.block0.size()) +
+                       align256(sizeof(KnobJob) * (kj.size() + 1));
+    // generous bound for the phase-2 tables (two split jobs and one group entry per problem)
+    tab_bytes += align256(sizeof(StageJob) * 2 * n) + align256(sizeof(int) * (2 * n + 1));
+    if (!h->gtab.ensure(tab_bytes)) return fail(h, OZGB_ERR_ALLOC, "grouped table buffer");
+    size_t toff = 0;
+    cudaMemsetAsync(gs, 0, total, st);  // column maxima and sums are accumulated atomically
+    const StageJob *dja = put_table(h, ja.jobs, &toff, st);
+    const int *dba = put_table(h, ja.block0, &toff, st);
+    if (h->profiling) cudaEventRecord(h->ev[0], st);
+    launch_stage_jobs(dja, dba, static_cast<int>(ja.jobs.size()), ja.total, st);
+    h->launches += 1;
+    if (h->profiling) cudaEventRecord(h->ev[1], st);
+
+    // ---- precision knob: one grouped reduction, one read-back
+    std::vector<int> s_pick(n, 0);
+    if (!kj.empty()) {
+        const KnobJob *dkj = put_table(h, kj, &toff, st);
+        launch_knob_grouped(dkj, static_cast<int>(kj.size()), st);
+        h->launches += 1;
+        std::vector<KnobStats> ks(n);
+        for (int i = 0; i < n; ++i)
+            if (bound[i] > 0.0) cudaMemcpyAsync(&ks[i], at(so[i].out), sizeof(KnobStats), cudaMemcpyDeviceToHost, st);
+        const cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return cuda_fail(h, e, "grouped statistics readback");
+        for (int i = 0; i < n; ++i)
+            if (bound[i] > 0.0) s_pick[i] = choose_slices_stats(ks[i], probs[i].K, 7, bound[i], 2, 16, nullptr);
+    }
+
+    // ---- plans
+    std::vector<Plan> plans(n);
+    for (int i = 0; i < n; ++i) {
+        OzConfig cfg = resolve_config(h, probs[i].K, mode);
+        if (s_pick[i] > 0) {
+            cfg.b = 7;
+            cfg.s = s_pick[i];
+            cfg.J = s_pick[i];
+        }
+        std::string why;
+        if (!make_plan(probs[i].M, probs[i].N, probs[i].K, cfg, &plans[i], &why))
+            return fail(h, OZGB_ERR_UNSUPPORTED, "problem " + std::to_string(i) + ": " + why);
+        probs[i].slices_used = plans[i].cfg.s;
+    }
+    // ---- stage (b): slice planes of every problem, one launch
+    std::vector<size_t> a_off(n), b_off(n);
+    size_t sl_total = 0;
+    for (int i = 0; i < n; ++i) {
+        a_off[i] = sl_total;
+        sl_total += align256(plans[i].a_elems * 2);
+        b_off[i] = sl_total;
+        sl_total += align256(plans[i].b_elems * 2);
+    }
+    if (!h->gslice.ensure(sl_total)) return fail(h, OZGB_ERR_ALLOC, "grouped slice buffer");
+    uint8_t *gsl = static_cast<uint8_t *>(h->gslice.p);
+    JobList jb;
+    for (int i = 0; i < n; ++i) {
+        const ozgb_problem &pb = probs[i];
+        const Plan &p = plans[i];
+        StageJob j{};
+        j.kind = JOB_SPLIT_A, j.X = pb.A, j.ld = pb.lda, j.rows = pb.M, j.cols = pb.K;
+        j.e_in = reinterpret_cast<int32_t *>(at(so[i].er));
+        j.b = p.cfg.b, j.s = p.cfg.s, j.KC = p.KC, j.n_kc = p.n_kc, j.padded = p.Mp, j.BN = p.BN;
+        j.tiles = reinterpret_cast<uint16_t *>(gsl + a_off[i]);
+        jb.add(j);
+        j.kind = JOB_SPLIT_B, j.X = pb.B, j.ld = pb.ldb, j.rows = pb.K, j.cols = pb.N;
+        j.e_in = reinterpret_cast<int32_t *>(at(so[i].ec));
+        j.padded = p.Np;
+        j.tiles = reinterpret_cast<uint16_t *>(gsl + b_off[i]);
+        jb.add(j);
+    }
+    jb.block0.push_back(jb.total);
+    const StageJob *djb = put_table(h, jb.jobs, &toff, st);
+    const int *dbb = put_table(h, jb.block0, &toff, st);
+    launch_stage_jobs(djb, dbb, static_cast<int>(jb.jobs.size()), jb.total, st);
+    h->launches += 1;
+    if (h->profiling) cudaEventRecord(h->ev[2], st);
+
+    // ---- stage (c)+(d): one persistent launch per problem; the launches are spread
+    // (largest first) over auxiliary streams forked from st, so that problems that
+    // fill few SMs run side by side
+    if (!h->ev_fork) {
+        bool okc = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) == cudaSuccess;
+        for (int a = 0; okc && a < ozgb_context::kAux; ++a)
+            okc = cudaStreamCreateWithFlags(&h->aux[a], cudaStreamNonBlocking) == cudaSuccess &&
+                  cudaEventCreateWithFlags(&h->ev_join[a], cudaEventDisableTiming) == cudaSuccess;
+        if (!okc) return cuda_fail(h, cudaGetLastError(), "auxiliary streams");
+    }
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        return static_cast<double>(plans[x].tiles_m) * plans[x].tiles_n * plans[x].n_kc * plans[x].pairs >
+               static_cast<double>(plans[y].tiles_m) * plans[y].tiles_n * plans[y].n_kc * plans[y].pairs;
+    });
+    const int n_aux = std::min(n, static_cast<int>(ozgb_context::kAux));
+    cudaEventRecord(h->ev_fork, st);
+    for (int a = 0; a < n_aux; ++a) cudaStreamWaitEvent(h->aux[a], h->ev_fork, 0);
+    for (int r = 0; r < n; ++r) {
+        const int k = order[r];
+        const Plan &p = plans[k];
+        GemmArgs g;
+        gemm_args_from_plan(&g, p, p.cfg.rounding, static_cast<int *>(h->err.p), h->timeout_ns);
+        g.a_tiles = reinterpret_cast<const uint16_t *>(gsl + a_off[k]);
+        g.b_tiles = reinterpret_cast<const uint16_t *>(gsl + b_off[k]);
+        g.er = reinterpret_cast<const int32_t *>(at(so[k].er));
+        g.ec = reinterpret_cast<const int32_t *>(at(so[k].ec));
+        g.c = probs[k].C;
+        g.ldc = probs[k].ldc;
+        g.M = probs[k].M;
+        g.N = probs[k].N;
+        g.n_kc = p.n_kc;
+        g.tiles_m = p.tiles_m;
+        g.tiles_n = p.tiles_n;
+        g.total_tiles = p.tiles_m * p.tiles_n;
+        p.fn(g, g.total_tiles, p.smem, h->aux[r % n_aux]);
+        h->launches += 1;
+    }
+    for (int a = 0; a < n_aux; ++a) {
+        cudaEventRecord(h->ev_join[a], h->aux[a]);
+        cudaStreamWaitEvent(st, h->ev_join[a], 0);
+    }
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(h, e, "grouped slice-pair GEMM launches");
+    if (h->profiling) {
+        cudaEventRecord(h->ev[3], st);
+        h->ev_recorded = true;
+    }
+    h->last = plans[n - 1];
+    h->have_last = true;
+    return OZGB_OK;
+}
+
 bool valid_mode(int mode) { return mode == OZGB_MODE_ACCURATE || mode == OZGB_MODE_FAST; }
 
 void fill_blocks(const Plan &p, ozgb_config *out) {
@@ -357,7 +620,7 @@ ozgb_status ozgb_release(ozgb_handle h) {
     std::lock_guard<std::mutex> lk(h->mu);
     if (h->device >= 0) cudaSetDevice(h->device);
     for (DevBuf *b : {&h->a, &h->b, &h->c, &h->at, &h->bt, &h->er, &h->ec, &h->ssr, &h->ssc, &h->raw, &h->knob, &h->kca,
-                      &h->krb, &h->ktmp})
+                      &h->krb, &h->ktmp, &h->gstat, &h->gslice, &h->gtab})
         b->release();
     h->setup_done = false;
     return OZGB_OK;
@@ -372,6 +635,11 @@ ozgb_status ozgb_destroy(ozgb_handle h) {
         for (auto &ev : h->ev)
             if (ev) cudaEventDestroy(ev);
         if (h->stream) cudaStreamDestroy(h->stream);
+        for (int i = 0; i < ozgb_context::kAux; ++i) {
+            if (h->aux[i]) cudaStreamDestroy(h->aux[i]);
+            if (h->ev_join[i]) cudaEventDestroy(h->ev_join[i]);
+        }
+        if (h->ev_fork) cudaEventDestroy(h->ev_fork);
     }
     delete h;
     return OZGB_OK;
@@ -457,19 +725,21 @@ ozgb_status ozgb_sync(ozgb_handle h) {
 
 ozgb_status ozgb_dgemm_grouped(ozgb_handle h, ozgb_problem *probs, int n, void *stream) {
     if (!h || (!probs && n > 0) || n < 0) return OZGB_ERR_ARG;
-    // First version: the problems run one after another on the stream (a fused
-    // grouped launch replaces this loop).
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (n == 0) return OZGB_OK;
     for (int i = 0; i < n; ++i) {
-        ozgb_problem &pb = probs[i];
-        double saved = h->err_bound;
-        if (pb.error_bound > 0) h->err_bound = pb.error_bound;
-        ozgb_status rc =
-            ozgb_dgemm_device(h, pb.M, pb.N, pb.K, pb.A, pb.lda, pb.B, pb.ldb, pb.C, pb.ldc, stream);
-        h->err_bound = saved;
-        if (rc) return rc;
-        pb.slices_used = h->last.cfg.s;
+        const ozgb_problem &pb = probs[i];
+        if (pb.M < 1 || pb.N < 1 || pb.K < 1) return fail(h, OZGB_ERR_DIMS, "problem dimensions must be positive");
+        if (!pb.A || !pb.B || !pb.C) return fail(h, OZGB_ERR_ARG, "null matrix pointer in a problem");
+        if (pb.lda < pb.K || pb.ldb < pb.N || pb.ldc < pb.N)
+            return fail(h, OZGB_ERR_ARG, "leading dimension too small in a problem");
     }
-    return OZGB_OK;
+    ozgb_status rc = ensure_device(h);
+    if (rc) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    h->last_stream = st;
+    const int mode = h->setup_done ? h->mode : OZGB_MODE_FAST;
+    return enqueue_grouped(h, probs, n, mode, st);
 }
 
 ozgb_status ozgb_set_profile(ozgb_handle h, int profile) {

@@ -293,17 +293,40 @@ struct DrainSchedule {
 #endif
 
 // ------------------------------------------------------------------ kernel
-// Grouped rasterisation: 8 M-tiles share the same stream of B tiles.
-__device__ __forceinline__ void tile_coords(const GemmArgs &g, int t, int *mt, int *nt) {
+// The operands and output of one tile and its position.  Grouped rasterisation:
+// 8 M-tiles share the same stream of B tiles.
+struct TileRef {
+    const uint8_t *a_src;
+    const uint8_t *b_src;
+    const int32_t *er;
+    const int32_t *ec;
+    double *c;
+    long ldc;
+    int M, N, n_kc, mt, nt;
+};
+
+__device__ __forceinline__ void tile_ref(const GemmArgs &g, int t, TileRef *r) {
+    r->er = g.er;
+    r->ec = g.ec;
+    r->c = g.c;
+    r->ldc = g.ldc;
+    r->M = g.M;
+    r->N = g.N;
+    r->n_kc = g.n_kc;
     const int GM = 8;
     const int per_group = GM * g.tiles_n;
     const int grp = t / per_group;
     const int first_m = grp * GM;
     const int gm = min(GM, g.tiles_m - first_m);
-    const int r = t - grp * per_group;
-    *mt = first_m + r % gm;
-    *nt = r / gm;
+    const int rr = t - grp * per_group;
+    r->mt = first_m + rr % gm;
+    r->nt = rr / gm;
+    r->a_src = reinterpret_cast<const uint8_t *>(g.a_tiles) + static_cast<size_t>(r->mt) * g.n_kc * g.a_block_bytes;
+    r->b_src = reinterpret_cast<const uint8_t *>(g.b_tiles) + static_cast<size_t>(r->nt) * g.n_kc * g.b_block_bytes;
 }
+
+// Stage mask value that ends the MMA issuer's loop (after the CTA's last tile).
+constexpr uint32_t kStageTerminate = 0x80000000u;
 
 // Persistent: CTA b processes tiles b, b + gridDim.x, ...  The stage ring, the
 // bin-block barriers and TMEM persist across tiles, so the producer prefetches
@@ -338,7 +361,6 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
     int *blk_np = reinterpret_cast<int *>(blk_id + kMaxGroups);             // A slices per UMMA run
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int n_tiles = g.tiles_m * g.tiles_n;
 #ifdef OZGB_PROBE
     long long pr0 = 0, pr1 = 0, pr2 = 0, pr3 = 0;
     const long long pstart = clock64();
@@ -383,49 +405,54 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
     if (warp == 0) {
         // ------------------------------------------------------ producer
         if (lane == 0) {
-            long long issued = 0;  // chunks issued by this CTA over all of its tiles
+            long long issued = 0;  // stage uses by this CTA over all of its tiles
             int st = 0;
             bool ok = true;
-            for (int t = blockIdx.x; ok && t < n_tiles; t += gridDim.x) {
-                int mt, nt;
-                tile_coords(g, t, &mt, &nt);
-                const uint8_t *a_src = reinterpret_cast<const uint8_t *>(g.a_tiles) +
-                                       static_cast<size_t>(mt) * g.n_kc * g.a_block_bytes;
-                const uint8_t *b_src = reinterpret_cast<const uint8_t *>(g.b_tiles) +
-                                       static_cast<size_t>(nt) * g.n_kc * g.b_block_bytes;
+            // waits until stage st may be refilled: use r (>= 1) of a stage waits for
+            // the (r-1)-th release of that stage
+            auto acquire = [&]() -> bool {
+                const long long r = issued / g.stages;
+                OZ_PT(tw);
+                const bool got = (r == 0) || mbar_wait(&empty[st], static_cast<uint32_t>((r - 1) & 1), vabort, TO);
+                OZ_PADD(pr0, tw);
+                if (!got && !*vabort) {
+                    atomicCAS(g.err, 0, DEVERR_TIMEOUT_PRODUCER);
+                    *vabort = 1;
+                }
+                return got;
+            };
+            for (int t = blockIdx.x; ok && t < g.total_tiles; t += gridDim.x) {
+                TileRef tr;
+                tile_ref(g, t, &tr);
                 DrainSchedule pds;
                 pds.init(g);
-                for (int c = 0; c < g.n_kc; ++c) {
-                    if (*vabort) {
-                        ok = false;
-                        break;
-                    }
-                    // use r of stage st (r >= 1) waits for the (r-1)-th release of that stage
-                    const long long r = issued / g.stages;
-                    OZ_PT(tw);
-                    const bool got = (r == 0) || mbar_wait(&empty[st], static_cast<uint32_t>((r - 1) & 1), vabort, TO);
-                    OZ_PADD(pr0, tw);
-                    if (!got) {
-                        if (!*vabort) {
-                            atomicCAS(g.err, 0, DEVERR_TIMEOUT_PRODUCER);
-                            *vabort = 1;
-                        }
+                for (int c = 0; c < tr.n_kc; ++c) {
+                    if (*vabort || !acquire()) {
                         ok = false;
                         break;
                     }
                     uint8_t *dst = smem + static_cast<size_t>(st) * g.stage_bytes;
-                    stage_mask[st] = pds.next(g, c == g.n_kc - 1);  // published by the arrive below
+                    stage_mask[st] = pds.next(g, c == tr.n_kc - 1);  // published by the arrive below
                     mbar_arrive_expect_tx(&full[st], g.a_block_bytes + g.b_block_bytes);
-                    bulk_g2s(dst, a_src + static_cast<size_t>(c) * g.a_block_bytes, g.a_block_bytes, &full[st]);
+                    bulk_g2s(dst, tr.a_src + static_cast<size_t>(c) * g.a_block_bytes, g.a_block_bytes, &full[st]);
                     bulk_g2s(dst + g.a_block_bytes + g.b_pad_lo_bytes,
-                             b_src + static_cast<size_t>(c) * g.b_block_bytes, g.b_block_bytes, &full[st]);
+                             tr.b_src + static_cast<size_t>(c) * g.b_block_bytes, g.b_block_bytes, &full[st]);
                     ++issued;
                     if (++st == g.stages) st = 0;
                 }
             }
-            // every copy issued must land before the CTA may exit
+            // end of work: one more stage use, without copies, tells the MMA issuer to stop
+            bool posted = false;
+            if (ok && !*vabort && acquire()) {
+                stage_mask[st] = kStageTerminate;
+                mbar_arrive(&full[st]);
+                posted = true;
+            }
+            // every copy issued must land before the CTA may exit (a stage reused by
+            // the terminate signal was consumed, so its copies have landed)
             const int zero = 0;
-            for (long long c = (issued > g.stages ? issued - g.stages : 0); c < issued; ++c)
+            const long long first = issued - g.stages + (posted ? 1 : 0);
+            for (long long c = (first > 0 ? first : 0); c < issued; ++c)
                 mbar_wait(&full[c % g.stages], static_cast<uint32_t>((c / g.stages) & 1), &zero, TO);
         }
     } else if (warp == 1) {
@@ -460,72 +487,71 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
             int st = 0;
             uint32_t fparity = 0;
             bool ok = true;
-            for (int t = blockIdx.x; ok && t < n_tiles; t += gridDim.x) {
-                for (int c = 0; ok && c < g.n_kc; ++c) {
-                    OZ_PT(tf);
-                    const bool gotf = mbar_wait(&full[st], fparity, vabort, TO);
-                    OZ_PADD(pr0, tf);
-                    if (!gotf) {
-                        ok = false;
-                        break;
-                    }
-                    tc_fence_after();
-                    OZ_PT(ti);
-                    const uint64_t stage_off = (static_cast<uint64_t>(st) * g.stage_bytes) >> 4;
-                    const uint32_t cur = stage_mask[st];
-                    // issue order: blocks drained after this chunk, then the rest, then the
-                    // blocks whose drain (after the previous chunk) must finish first
-                    uint32_t order[3] = {cur & ~prev, all & ~cur & ~prev, prev};
-                    for (int cls = 0; ok && cls < 3; ++cls) {
-                        uint32_t m = order[cls];
-                        while (m) {
-                            const int blk = __ffs(m) - 1;
-                            const uint32_t bit = 1u << blk;
-                            m &= m - 1;
-                            if (cls == 2) {
-                                OZ_PT(te);
-                                const bool gote = mbar_wait(&gempty[blk],
-                                                            static_cast<uint32_t>((ephase >> blk) & 1ull), vabort, TO);
-                                OZ_PADD(pr1, te);
-                                if (!gote) {
-                                    ok = false;
-                                    break;
-                                }
-                                ephase ^= (1ull << blk);
-                                tc_fence_after();
+            for (;;) {
+                OZ_PT(tf);
+                const bool gotf = mbar_wait(&full[st], fparity, vabort, TO);
+                OZ_PADD(pr0, tf);
+                if (!gotf) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                OZ_PT(ti);
+                const uint64_t stage_off = (static_cast<uint64_t>(st) * g.stage_bytes) >> 4;
+                const uint32_t cur = stage_mask[st];
+                if (cur & kStageTerminate) break;
+                // issue order: blocks drained after this chunk, then the rest, then the
+                // blocks whose drain (after the previous chunk) must finish first
+                uint32_t order[3] = {cur & ~prev, all & ~cur & ~prev, prev};
+                for (int cls = 0; ok && cls < 3; ++cls) {
+                    uint32_t m = order[cls];
+                    while (m) {
+                        const int blk = __ffs(m) - 1;
+                        const uint32_t bit = 1u << blk;
+                        m &= m - 1;
+                        if (cls == 2) {
+                            OZ_PT(te);
+                            const bool gote = mbar_wait(&gempty[blk],
+                                                        static_cast<uint32_t>((ephase >> blk) & 1ull), vabort, TO);
+                            OZ_PADD(pr1, te);
+                            if (!gote) {
+                                ok = false;
+                                break;
                             }
-                            const uint32_t d_tmem = blk_tm[blk];
-                            const uint32_t idesc = blk_id[blk];
-                            const int np = blk_np[blk];
-                            uint64_t ad = blk_ad[blk] + stage_off;
-                            uint64_t bd = blk_bd[blk] + stage_off;
-                            uint32_t acc = (fresh & bit) ? 0u : 1u;
-                            for (int p = 0; p < np; ++p) {
+                            ephase ^= (1ull << blk);
+                            tc_fence_after();
+                        }
+                        const uint32_t d_tmem = blk_tm[blk];
+                        const uint32_t idesc = blk_id[blk];
+                        const int np = blk_np[blk];
+                        uint64_t ad = blk_ad[blk] + stage_off;
+                        uint64_t bd = blk_bd[blk] + stage_off;
+                        uint32_t acc = (fresh & bit) ? 0u : 1u;
+                        for (int p = 0; p < np; ++p) {
 #pragma unroll
-                                for (int kk = 0; kk < ksteps; ++kk) {
-                                    umma_bf16(d_tmem, ad + static_cast<uint64_t>(kk * 16),
-                                              bd + static_cast<uint64_t>(kk * 16), idesc, acc);
-                                    acc = 1u;
-                                }
-                                ad += a_step;
-                                bd -= b_step;
+                            for (int kk = 0; kk < ksteps; ++kk) {
+                                umma_bf16(d_tmem, ad + static_cast<uint64_t>(kk * 16),
+                                          bd + static_cast<uint64_t>(kk * 16), idesc, acc);
+                                acc = 1u;
                             }
-                            fresh &= ~bit;
-                            if (cur & bit) {
-                                umma_commit(&gfull[blk]);
-                                fresh |= bit;
-                            }
+                            ad += a_step;
+                            bd -= b_step;
+                        }
+                        fresh &= ~bit;
+                        if (cur & bit) {
+                            umma_commit(&gfull[blk]);
+                            fresh |= bit;
                         }
                     }
-                    OZ_PADD(pr2, ti);
-                    if (!ok) break;
-                    umma_commit(&empty[st]);
-                    if (++st == g.stages) {
-                        st = 0;
-                        fparity ^= 1u;
-                    }
-                    prev = cur;
                 }
+                OZ_PADD(pr2, ti);
+                if (!ok) break;
+                umma_commit(&empty[st]);
+                if (++st == g.stages) {
+                    st = 0;
+                    fparity ^= 1u;
+                }
+                prev = cur;
             }
             if (!ok && !*vabort) {
                 atomicCAS(g.err, 0, DEVERR_TIMEOUT_MMA);
@@ -548,9 +574,9 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
         uint64_t fphase = 0;
         uint32_t prev = 0;
         bool ok = true;
-        for (int t = blockIdx.x; ok && t < n_tiles; t += gridDim.x) {
-            int mt, nt;
-            tile_coords(g, t, &mt, &nt);
+        for (int t = blockIdx.x; ok && t < g.total_tiles; t += gridDim.x) {
+            TileRef tr;
+            tile_ref(g, t, &tr);
 #pragma unroll
             for (int i = 0; i < COLS; ++i)
 #pragma unroll
@@ -558,8 +584,8 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
 
             DrainSchedule ds;
             ds.init(g);
-            for (int c = 0; ok && c < g.n_kc; ++c) {
-                const bool last = (c == g.n_kc - 1);
+            for (int c = 0; ok && c < tr.n_kc; ++c) {
+                const bool last = (c == tr.n_kc - 1);
                 const uint32_t cur = ds.next(g, last);
                 for (int pass = 0; ok && pass < 2; ++pass) {
                     uint32_t m = pass == 0 ? (cur & ~prev) : (cur & prev);
@@ -610,28 +636,28 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
 
             // --------------------------------------------------- epilogue
             OZ_PT(tq);
-            const int row = mt * BM + 32 * qd + lane;
-            const int col0 = nt * BN + part * COLS;
-            if (row < g.M) {
-                const int er = g.er[row];
+            const int row = tr.mt * BM + 32 * qd + lane;
+            const int col0 = tr.nt * BN + part * COLS;
+            if (row < tr.M) {
+                const int er = tr.er[row];
                 const int bJ1 = g.b * (g.J + 1);
                 if (g.out_mode == OUT_RAW) {
 #pragma unroll
                     for (int i = 0; i < COLS; ++i) {
                         const int col = col0 + i;
-                        if (col < g.N) {
-                            int32_t *dst = g.raw + (static_cast<size_t>(row) * g.N + col) * 4;
+                        if (col < tr.N) {
+                            int32_t *dst = g.raw + (static_cast<size_t>(row) * tr.N + col) * 4;
                             const uint32_t ext = static_cast<uint32_t>(static_cast<int32_t>(q[i][W - 1]) >> 31);
 #pragma unroll
                             for (int w = 0; w < 4; ++w) dst[w] = static_cast<int32_t>(w < W ? q[i][w] : ext);
                         }
                     }
                 } else {
-                    double *crow = g.c + static_cast<size_t>(row) * g.ldc;
+                    double *crow = tr.c + static_cast<size_t>(row) * tr.ldc;
 #pragma unroll
                     for (int i = 0; i < COLS; ++i) {
                         const int col = col0 + i;
-                        if (col < g.N) crow[col] = q_to_double<W>(q[i], er + g.ec[col], bJ1, g.out_mode);
+                        if (col < tr.N) crow[col] = q_to_double<W>(q[i], er + tr.ec[col], bJ1, g.out_mode);
                     }
                 }
             }
@@ -676,7 +702,8 @@ template <int BN, int W, int KC>
 void launch_gemm_variant(const GemmArgs &args, int tiles, size_t smem, void *stream) {
     auto kern = oz_gemm_kernel<BN, W, KC>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    const int grid = tiles < device_sm_count() ? tiles : device_sm_count();
+    const int grid = args.total_tiles < device_sm_count() ? args.total_tiles : device_sm_count();
+    (void)tiles;
     kern<<<grid, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(args);
 }
 

@@ -69,6 +69,38 @@ struct GemmArgs {
     int G;
     int blk_lo[kMaxGroups], blk_nb[kMaxGroups], blk_p0[kMaxGroups], blk_p1[kMaxGroups];
     int blk_period[kMaxGroups], blk_off[kMaxGroups];
+    int total_tiles;  // tiles_m * tiles_n
+};
+
+// Work items of the grouped stage-(a)/(b) launch (k_stage_jobs): each job is one
+// of the per-problem kernels below, run on blocks [block0, block0 + gx * gy) of
+// the launch with local block coordinates (bx, by).
+enum StageKind : int { JOB_ROWMAX = 0, JOB_COLMAX = 1, JOB_SPLIT_A = 2, JOB_SPLIT_B = 3 };
+struct StageJob {
+    int kind, gx, gy;
+    const double *X;     // A (M x K) or B (K x N), row-major
+    long ld;
+    int rows, cols;      // of X
+    int32_t *e_out;      // ROWMAX / COLMAX: exponent fields (may be null)
+    double *ss_out;      // ROWMAX / COLMAX: sums of squares (may be null)
+    const int32_t *e_in; // SPLIT: row (A) / column (B) exponents
+    int b, s, KC, n_kc, padded, BN;  // SPLIT: padded = Mp (A) or Np (B)
+    uint16_t *tiles;
+};
+constexpr int kStageThreads = 256;
+
+// Per-problem inputs of the grouped precision-knob reduction (3 blocks each).
+struct KnobJob {
+    const int32_t *er;
+    const double *ssr;
+    int M;
+    const int32_t *ec;
+    const double *ssc;
+    int N;
+    const double *ca;
+    const double *rb;
+    int K;
+    double *out;  // 5 doubles
 };
 
 // Device error codes written to the error word.
@@ -99,5 +131,11 @@ int launch_selftest_timeout(int *err, unsigned long long timeout_ns, void *strea
 // squares ca[k] = |A(:,k)|^2, rb[k] = |B(k,:)|^2.
 void launch_knob_stats(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N,
                        const double *ca, const double *rb, int K, double *out, void *stream);
+// Grid sizes of the per-problem stage kernels (blocks in x and y of 256 threads).
+void stage_grid(const StageJob &j, int *gx, int *gy);
+// Grouped launches: all jobs in one grid (block0[i] = first block of job i,
+// block0[n_jobs] = total), and the knob reduction of n problems.
+void launch_stage_jobs(const StageJob *jobs, const int *block0, int n_jobs, int total_blocks, void *stream);
+void launch_knob_grouped(const KnobJob *jobs, int n, void *stream);
 
 }  // namespace ozgb

@@ -134,6 +134,7 @@ extern "C" ozgb_status ozgb_dgemm_device_noalloc(int M, int N, int K, const doub
     g.out_mode = OUT_RN;
     g.tiles_m = p.tiles_m;
     g.tiles_n = p.tiles_n;
+    g.total_tiles = p.tiles_m * p.tiles_n;
     g.stages = p.stages;
     g.stage_bytes = p.stage_bytes;
     g.a_block_bytes = p.a_block_bytes;

@@ -21,9 +21,9 @@ __device__ __forceinline__ int exp_field(double x) {
 
 // ------------------------------------------------------------- stage (a)
 // One warp per row of A: max exponent field (and sum of squares when ss != null).
-__global__ void k_rowmax(const double *__restrict__ A, long lda, int M, int K, int32_t *__restrict__ er,
-                         double *__restrict__ ss) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__device__ __forceinline__ void rowmax_body(const double *__restrict__ A, long lda, int M, int K, int32_t *__restrict__ er,
+                         double *__restrict__ ss, int bx, int by) {
+    const int warp = (bx * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= M) return;
     const double *row = A + static_cast<size_t>(warp) * lda;
@@ -40,18 +40,22 @@ __global__ void k_rowmax(const double *__restrict__ A, long lda, int M, int K, i
         if (ss) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
     }
     if (lane == 0) {
-        er[warp] = e;
+        if (er) er[warp] = e;
         if (ss) ss[warp] = s2;
     }
+}
+__global__ void k_rowmax(const double *__restrict__ A, long lda, int M, int K, int32_t *__restrict__ er,
+                         double *__restrict__ ss) {
+    rowmax_body(A, lda, M, K, er, ss, blockIdx.x, blockIdx.y);
 }
 
 // One thread per column of B over a slab of rows; combined with atomicMax
 // (ec must be zeroed first) and, when ss != null, atomicAdd of squares.
-__global__ void k_colmax(const double *__restrict__ B, long ldb, int K, int N, int rows_per_slab,
-                         int32_t *__restrict__ ec, double *__restrict__ ss) {
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void colmax_body(const double *__restrict__ B, long ldb, int K, int N, int rows_per_slab,
+                         int32_t *__restrict__ ec, double *__restrict__ ss, int bx, int by) {
+    const int n = bx * blockDim.x + threadIdx.x;
     if (n >= N) return;
-    const int k0 = blockIdx.y * rows_per_slab;
+    const int k0 = by * rows_per_slab;
     const int k1 = min(K, k0 + rows_per_slab);
     int e = 0;
     double s2 = 0.0;
@@ -60,8 +64,12 @@ __global__ void k_colmax(const double *__restrict__ B, long ldb, int K, int N, i
         e = max(e, exp_field(x));
         if (ss) s2 = fma(x, x, s2);
     }
-    atomicMax(ec + n, e);
+    if (ec) atomicMax(ec + n, e);
     if (ss) atomicAdd(ss + n, s2);
+}
+__global__ void k_colmax(const double *__restrict__ B, long ldb, int K, int N, int rows_per_slab,
+                         int32_t *__restrict__ ec, double *__restrict__ ss) {
+    colmax_body(B, ldb, K, N, rows_per_slab, ec, ss, blockIdx.x, blockIdx.y);
 }
 
 // ------------------------------------------------------------- stage (b)
@@ -116,12 +124,12 @@ __host__ __device__ inline bool split_two_windows(int b, int s) {
 // A [M][K] row-major -> A slice blocks [mt][c][p][128 x KC].  One thread takes 8
 // consecutive K values of one row and writes one 16-byte piece per slice; a warp
 // covers 8 rows x 32 K (4 core matrices of each slice, 512 contiguous bytes).
-__global__ void k_split_a(const double *__restrict__ A, long lda, int M, int K, const int32_t *__restrict__ er,
-                          int b, int s, int KC, int n_kc, int Mp, uint16_t *__restrict__ tiles) {
+__device__ __forceinline__ void split_a_body(const double *__restrict__ A, long lda, int M, int K, const int32_t *__restrict__ er,
+                          int b, int s, int KC, int n_kc, int Mp, uint16_t *__restrict__ tiles, int bx, int by) {
     const int r8 = threadIdx.x & 7;
     const int kgl = threadIdx.x >> 3;  // 0..31
-    const int m = blockIdx.y * 8 + r8;
-    const int k0 = (blockIdx.x * 32 + kgl) * 8;
+    const int m = by * 8 + r8;
+    const int k0 = (bx * 32 + kgl) * 8;
     const int Kp = n_kc * KC;
     if (m >= Mp || k0 >= Kp) return;
     const bool two = split_two_windows(b, s);
@@ -146,14 +154,18 @@ __global__ void k_split_a(const double *__restrict__ A, long lda, int M, int K, 
         *reinterpret_cast<uint4 *>(dst + p * slice_elems) = v;
     }
 }
+__global__ void k_split_a(const double *__restrict__ A, long lda, int M, int K, const int32_t *__restrict__ er,
+                          int b, int s, int KC, int n_kc, int Mp, uint16_t *__restrict__ tiles) {
+    split_a_body(A, lda, M, K, er, b, s, KC, n_kc, Mp, tiles, blockIdx.x, blockIdx.y);
+}
 
 // B [K][N] row-major -> slice blocks of B^T [nt][c][q][BN x KC].  One thread
 // takes one column n and 8 consecutive K; a warp reads 32 consecutive columns
 // per row (coalesced) and writes four 128-byte core matrices per slice.
-__global__ void k_split_b(const double *__restrict__ B, long ldb, int K, int N, const int32_t *__restrict__ ec,
-                          int b, int s, int KC, int n_kc, int BN, int Np, uint16_t *__restrict__ tiles) {
-    const int n = blockIdx.x * 32 + (threadIdx.x & 31);
-    const int k0 = (blockIdx.y * 8 + (threadIdx.x >> 5)) * 8;
+__device__ __forceinline__ void split_b_body(const double *__restrict__ B, long ldb, int K, int N, const int32_t *__restrict__ ec,
+                          int b, int s, int KC, int n_kc, int BN, int Np, uint16_t *__restrict__ tiles, int bx, int by) {
+    const int n = bx * 32 + (threadIdx.x & 31);
+    const int k0 = (by * 8 + (threadIdx.x >> 5)) * 8;
     const int Kp = n_kc * KC;
     if (n >= Np || k0 >= Kp) return;
     const bool two = split_two_windows(b, s);
@@ -176,6 +188,10 @@ __global__ void k_split_b(const double *__restrict__ B, long ldb, int K, int N, 
         v.w = slice_bf16(st[6], q, b) | (slice_bf16(st[7], q, b) << 16);
         *reinterpret_cast<uint4 *>(dst + q * slice_elems) = v;
     }
+}
+__global__ void k_split_b(const double *__restrict__ B, long ldb, int K, int N, const int32_t *__restrict__ ec,
+                          int b, int s, int KC, int n_kc, int BN, int Np, uint16_t *__restrict__ tiles) {
+    split_b_body(B, ldb, K, N, ec, b, s, KC, n_kc, BN, Np, tiles, blockIdx.x, blockIdx.y);
 }
 
 // A kernel whose only wait is on an mbarrier that nothing arrives on: exercises
@@ -224,26 +240,26 @@ __device__ double block_sum(double v, double *sh) {
 //   out[2] = sum_j 4^{Ec_j-eb}           out[3] = sum_j |b_j|^2 4^{1022-eb}
 //   out[4] = sum_k |A(:,k)|^2 |B(k,:)|^2 4^{2044-ea-eb}
 // Block 0 makes the A terms, block 1 the B terms, block 2 the K-direction term.
-__global__ void k_knob_stats(const int32_t *__restrict__ er, const double *__restrict__ ssr, int M,
-                             const int32_t *__restrict__ ec, const double *__restrict__ ssc, int N,
-                             const double *__restrict__ ca, const double *__restrict__ rb, int K,
-                             double *__restrict__ out) {
+__device__ __forceinline__ void knob_stats_body(const int32_t *__restrict__ er, const double *__restrict__ ssr, int M,
+                                                const int32_t *__restrict__ ec, const double *__restrict__ ssc, int N,
+                                                const double *__restrict__ ca, const double *__restrict__ rb, int K,
+                                                double *__restrict__ out, const int role) {
     __shared__ int sh_i[32];
     __shared__ double sh_d[32];
     int ea = 0, eb = 0;
-    if (blockIdx.x != 1) {
+    if (role != 1) {
         for (int i = threadIdx.x; i < M; i += blockDim.x) ea = max(ea, er[i]);
         ea = block_max_int(ea, sh_i);
     }
-    if (blockIdx.x != 0) {
+    if (role != 0) {
         for (int j = threadIdx.x; j < N; j += blockDim.x) eb = max(eb, ec[j]);
         eb = block_max_int(eb, sh_i);
     }
-    if (blockIdx.x < 2) {
-        const int32_t *e = blockIdx.x == 0 ? er : ec;
-        const double *ss = blockIdx.x == 0 ? ssr : ssc;
-        const int n = blockIdx.x == 0 ? M : N;
-        const int emax = blockIdx.x == 0 ? ea : eb;
+    if (role < 2) {
+        const int32_t *e = role == 0 ? er : ec;
+        const double *ss = role == 0 ? ssr : ssc;
+        const int n = role == 0 ? M : N;
+        const int emax = role == 0 ? ea : eb;
         double num = 0.0, den = 0.0;
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             num += ldexp(1.0, 2 * (e[i] - emax));
@@ -252,8 +268,8 @@ __global__ void k_knob_stats(const int32_t *__restrict__ er, const double *__res
         num = block_sum(num, sh_d);
         den = block_sum(den, sh_d);
         if (threadIdx.x == 0) {
-            out[2 * blockIdx.x] = num;
-            out[2 * blockIdx.x + 1] = den;
+            out[2 * role] = num;
+            out[2 * role + 1] = den;
         }
     } else {
         double t = 0.0;
@@ -265,6 +281,75 @@ __global__ void k_knob_stats(const int32_t *__restrict__ er, const double *__res
 }
 
 // ---------------------------------------------------------------- launches
+__global__ void k_knob_stats(const int32_t *__restrict__ er, const double *__restrict__ ssr, int M,
+                             const int32_t *__restrict__ ec, const double *__restrict__ ssc, int N,
+                             const double *__restrict__ ca, const double *__restrict__ rb, int K,
+                             double *__restrict__ out) {
+    knob_stats_body(er, ssr, M, ec, ssc, N, ca, rb, K, out, blockIdx.x);
+}
+
+// Grouped knob reduction: blocks 3p, 3p+1, 3p+2 reduce problem p.
+__global__ void k_knob_grouped(const KnobJob *__restrict__ jobs) {
+    const KnobJob j = jobs[blockIdx.x / 3];
+    knob_stats_body(j.er, j.ssr, j.M, j.ec, j.ssc, j.N, j.ca, j.rb, j.K, j.out, blockIdx.x % 3);
+}
+
+// Grouped stage (a)/(b): block -> job by binary search over block0[], then the
+// job's per-problem kernel body with its local block coordinates.
+__global__ void __launch_bounds__(kStageThreads) k_stage_jobs(const StageJob *__restrict__ jobs,
+                                                              const int *__restrict__ block0, int n_jobs) {
+    int lo = 0, hi = n_jobs - 1;
+    const int bid = blockIdx.x;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(block0 + mid) <= bid) lo = mid;
+        else hi = mid - 1;
+    }
+    const StageJob &j = jobs[lo];
+    const int local = bid - __ldg(block0 + lo);
+    const int bx = local % j.gx, by = local / j.gx;
+    switch (j.kind) {
+        case JOB_ROWMAX: rowmax_body(j.X, j.ld, j.rows, j.cols, j.e_out, j.ss_out, bx, by); break;
+        case JOB_COLMAX: colmax_body(j.X, j.ld, j.rows, j.cols, 64, j.e_out, j.ss_out, bx, by); break;
+        case JOB_SPLIT_A:
+            split_a_body(j.X, j.ld, j.rows, j.cols, j.e_in, j.b, j.s, j.KC, j.n_kc, j.padded, j.tiles, bx, by);
+            break;
+        default:
+            split_b_body(j.X, j.ld, j.rows, j.cols, j.e_in, j.b, j.s, j.KC, j.n_kc, j.BN, j.padded, j.tiles, bx, by);
+            break;
+    }
+}
+
+void stage_grid(const StageJob &j, int *gx, int *gy) {
+    switch (j.kind) {
+        case JOB_ROWMAX:
+            *gx = (j.rows * 32 + kStageThreads - 1) / kStageThreads;
+            *gy = 1;
+            break;
+        case JOB_COLMAX:
+            *gx = (j.cols + kStageThreads - 1) / kStageThreads;
+            *gy = (j.rows + 63) / 64;
+            break;
+        case JOB_SPLIT_A:
+            *gx = (j.n_kc * j.KC / 8 + 31) / 32;
+            *gy = j.padded / 8;
+            break;
+        default:
+            *gx = (j.padded + 31) / 32;
+            *gy = (j.n_kc * j.KC / 8 + 7) / 8;
+            break;
+    }
+}
+
+void launch_stage_jobs(const StageJob *jobs, const int *block0, int n_jobs, int total_blocks, void *stream) {
+    if (total_blocks > 0)
+        k_stage_jobs<<<total_blocks, kStageThreads, 0, static_cast<cudaStream_t>(stream)>>>(jobs, block0, n_jobs);
+}
+
+void launch_knob_grouped(const KnobJob *jobs, int n, void *stream) {
+    if (n > 0) k_knob_grouped<<<3 * n, 1024, 0, static_cast<cudaStream_t>(stream)>>>(jobs);
+}
+
 void launch_knob_stats(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N,
                        const double *ca, const double *rb, int K, double *out, void *stream) {
     k_knob_stats<<<3, 1024, 0, static_cast<cudaStream_t>(stream)>>>(er, ssr, M, ec, ssc, N, ca, rb, K, out);
