@@ -158,6 +158,86 @@ def cpu_blas_dgemm(A, B):
     return {"value": 2.0 * 1024 * N * K / dt / 1e12, "unit": UNIT, "sample": "1024 x 4096 x 4096"}
 
 
+def batched_workload(n, seed=7, lo=32, hi=2048):
+    """Sizes of the batched workload: M, N, K each log-uniform in [lo, hi]."""
+    g = np.random.default_rng(seed)
+    return np.exp(g.uniform(np.log(lo), np.log(hi), size=(n, 3))).astype(np.int64)
+
+
+def batched_run(n_probs, dev, stream, oz, O, torch):
+    """Many uneven DGEMMs: the grouped, accuracy-adaptive call (replayed CUDA
+    graphs) against plain per-call DGEMMs with the fixed accurate configuration
+    (s = 8, full pair set), both on device-resident operands."""
+    sizes = batched_workload(n_probs)
+    probs, hosts, flops = [], [], 0.0
+    for i, (m, n, k) in enumerate(sizes):
+        m, n, k = int(m), int(n), int(k)
+        A = O.gen_phi((m, k), 10000 + i, PHI)
+        B = O.gen_phi((k, n), 20000 + i, PHI)
+        dA, dB = torch.from_numpy(A).to(dev), torch.from_numpy(B).to(dev)
+        dC = torch.empty((m, n), dtype=torch.float64, device=dev)
+        probs.append({"M": m, "N": n, "K": k, "A": dA.data_ptr(), "lda": k, "B": dB.data_ptr(), "ldb": n,
+                      "C": dC.data_ptr(), "ldc": n, "error_bound": BOUND})
+        hosts.append((A, B, dA, dB, dC))
+        flops += 2.0 * m * n * k
+    hg = oz.Handle()
+    hg.set_graph(1)
+
+    def grouped():
+        rc, used = hg.dgemm_grouped(probs, stream.cuda_stream)
+        if rc:
+            raise RuntimeError(hg.last_error())
+        return used
+
+    for _ in range(3):
+        used = grouped()
+    torch.cuda.synchronize()
+    reps = 5
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        grouped()
+    torch.cuda.synchronize()
+    g_ms = (time.perf_counter() - t0) / reps * 1e3
+    if hg.sync():
+        raise RuntimeError(hg.last_error())
+    # accuracy: 64 sampled entries of 8 problems against the exact products
+    worst = 0.0
+    for i in range(0, n_probs, max(1, n_probs // 8)):
+        A, B, _, _, dC = hosts[i]
+        r, c = O.sample_indices(A.shape[0], B.shape[1], 64, i)
+        ex, _ = O.exact_entries(A, B, r, c)
+        got = dC.cpu().numpy()[r, c]
+        worst = max(worst, float(np.linalg.norm(got - ex) / max(np.linalg.norm(ex), 1e-300)))
+    hg.close()
+
+    hp = oz.Handle()
+    hp.set_slices(8)
+    hp.set_bins(15)
+
+    def plain():
+        for pb in probs:
+            if hp.dgemm_device(pb["M"], pb["N"], pb["K"], pb["A"], pb["lda"], pb["B"], pb["ldb"], pb["C"], pb["ldc"],
+                               stream.cuda_stream):
+                raise RuntimeError(hp.last_error())
+
+    plain()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(2):
+        plain()
+    torch.cuda.synchronize()
+    p_ms = (time.perf_counter() - t0) / 2 * 1e3
+    hp.close()
+    return {"workload": "%d DGEMMs, M, N, K log-uniform in [32, 2048] (seed 7), phi=1, bound 1e-15 each" % n_probs,
+            "effective_flop": flops,
+            "grouped_adaptive_graph": {"value": flops / (g_ms * 1e-3) / 1e12, "unit": UNIT, "ms": g_ms,
+                                       "slices_hist": {str(k): int(v) for k, v in
+                                                       zip(*np.unique(used, return_counts=True))},
+                                       "max_normwise_rel_err_sampled": worst},
+            "plain_per_call_s8_full": {"value": flops / (p_ms * 1e-3) / 1e12, "unit": UNIT, "ms": p_ms},
+            "speedup": p_ms / g_ms}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -199,6 +279,7 @@ def main():
                     help="only the timed DGEMM steps (for ncu launch lists and captures)")
     ap.add_argument("--case", type=int, default=0, help="square size for --profile-only (default 4096)")
     ap.add_argument("--slices", type=int, default=0, help="fixed triangular slice count for --profile-only")
+    ap.add_argument("--batched", type=int, default=512, help="problems in the batched comparison (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -342,6 +423,8 @@ def main():
     cublas_ms = c0.elapsed_time(c1) / 3
     err_cublas = O.error_report(dC.cpu().numpy(), A, B, r, c, exact, absdot)
 
+    batched = batched_run(args.batched, dev, stream, oz, O, torch) if args.batched > 0 and rank == 0 else None
+
     peaks = load_peaks()
     mma_flops = 2.0 * cfg["pairs"] * M * N * K
     achieved = mma_flops / (gemm_ms * 1e-3) / 1e12
@@ -371,6 +454,7 @@ def main():
                          "peak_source": peaks["source"] + " bf16 burst (cuBLAS)",
                          "algorithmic": "2 * pairs * M * N * K bf16 MMA flops per launch"},
             "gpu_launches": gpu_launches,
+            "batched": batched,
             "clocks": clk,
         }
         if not args.no_cpu_baseline:

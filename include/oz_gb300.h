@@ -128,9 +128,17 @@ typedef struct {
     double error_bound; /* requested normwise relative error; <= 0: use the handle's slices */
     int slices_used;    /* out: slices chosen for this problem */
 } ozgb_problem;
-/* Many independent DGEMMs: one grouped launch per stage for all problems
- * (optionally captured once into a CUDA graph and replayed, see
- * ozgb_set_graph).  Enqueued on `stream`. */
+/* Many independent DGEMMs of any sizes (the spec batched form; the
+ * reference runs one ozAIE_DGEMM per call, include/oz_aie.h:311).  One launch
+ * computes the exponents of every problem, one the splits of every problem; the
+ * slice-pair GEMMs run per problem, largest first, on auxiliary streams forked
+ * from and joined back into `stream`.  Problems with an error bound get their
+ * slice count from the precision knob: the call then waits once for the knob's
+ * statistics of all problems.  With ozgb_set_graph(h, 1) both halves are
+ * captured into CUDA graphs and replayed while the problem list (sizes,
+ * pointers, bounds) and the chosen slice counts stay the same.  The handle's
+ * grouped buffers serve one call at a time: calls on one handle must not
+ * overlap on the GPU. */
 ozgb_status ozgb_dgemm_grouped(ozgb_handle h, ozgb_problem *probs, int n, void *stream);
 
 /* ---------------------------------------------------------------- options */
@@ -142,7 +150,7 @@ ozgb_status ozgb_set_rounding(ozgb_handle h, int rounding);
 /* Requested normwise relative error (> 0 enables slice selection from the
  * exponent spread measured by stage (a)); 0 disables it. */
 ozgb_status ozgb_set_error_bound(ozgb_handle h, double bound);
-ozgb_status ozgb_set_graph(ozgb_handle h, int enable);     /* capture grouped launches in a CUDA graph */
+ozgb_status ozgb_set_graph(ozgb_handle h, int enable);     /* capture grouped calls in CUDA graphs */
 ozgb_status ozgb_set_timeout_ms(ozgb_handle h, double ms); /* device-side wait limit, default 2000 */
 ozgb_status ozgb_get_config(ozgb_handle h, ozgb_config *out);
 /* Per-stage device times of the last call (ms): [0] exponents, [1] split,

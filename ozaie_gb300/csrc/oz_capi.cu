@@ -75,6 +75,12 @@ struct ozgb_context {
     cudaStream_t aux[kAux] = {};
     cudaEvent_t ev_fork = nullptr;
     cudaEvent_t ev_join[kAux] = {};
+    // grouped calls under CUDA graphs (ozgb_set_graph): the two captured phases and
+    // the inputs they were captured for; the knob statistics land in pinned memory
+    std::vector<long long> gkey1, gkey2;
+    cudaGraphExec_t gexec1 = nullptr, gexec2 = nullptr;
+    KnobStats *knob_host = nullptr;
+    size_t knob_host_n = 0;
     cudaStream_t last_stream = nullptr;  // stream of the last enqueued call
     // profiling
     bool profiling = false;
@@ -384,27 +390,73 @@ struct JobList {
     }
 };
 
+// Runs enqueue(stream) directly on st, or, with graphs enabled, replays the graph
+// captured for the same key (capturing it first when the key changed).
+template <typename F>
+ozgb_status run_phase(ozgb_handle h, bool graph, const std::vector<long long> &key, std::vector<long long> *cached_key,
+                      cudaGraphExec_t *exec, cudaStream_t st, F enqueue) {
+    if (!graph) return enqueue(st);
+    if (*exec && *cached_key == key) {
+        const cudaError_t e = cudaGraphLaunch(*exec, st);
+        return e == cudaSuccess ? OZGB_OK : cuda_fail(h, e, "graph launch");
+    }
+    if (*exec) {
+        cudaGraphExecDestroy(*exec);
+        *exec = nullptr;
+    }
+    cached_key->clear();
+    // capture on the handle's own stream (the caller's may be the legacy default
+    // stream, which cannot be captured), then launch on the caller's stream
+    cudaStream_t cs = h->stream;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) return cuda_fail(h, e, "begin capture");
+    const ozgb_status rc = enqueue(cs);
+    cudaGraph_t graph_ = nullptr;
+    e = cudaStreamEndCapture(cs, &graph_);
+    if (rc != OZGB_OK) {
+        if (graph_) cudaGraphDestroy(graph_);
+        return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(h, e, "end capture");
+    e = cudaGraphInstantiate(exec, graph_, 0);
+    cudaGraphDestroy(graph_);
+    if (e != cudaSuccess) {
+        *exec = nullptr;
+        return cuda_fail(h, e, "graph instantiate");
+    }
+    *cached_key = key;
+    e = cudaGraphLaunch(*exec, st);
+    return e == cudaSuccess ? OZGB_OK : cuda_fail(h, e, "graph launch");
+}
+
 // The grouped pipeline: one launch for every problem's stage (a) (and the knob's
 // statistics), one grouped knob reduction and a single read-back when any
-// problem asks for an error bound, one launch for every problem's split, and one
-// persistent slice-pair GEMM launch per class of problems sharing a plan.
+// problem asks for an error bound, one launch for every problem's split, and the
+// persistent slice-pair GEMMs.  With graphs enabled both halves are captured once
+// and replayed while the problems (and, for the second half, the slice counts)
+// stay the same.
 ozgb_status enqueue_grouped(ozgb_handle h, ozgb_problem *probs, int n, int mode, cudaStream_t st) {
+    const bool graph = h->use_graph != 0;
+    const bool prof = h->profiling && !graph;
     std::vector<double> bound(n, 0.0);
+    std::vector<int> adapt_idx(n, -1);
     int n_adapt = 0;
     for (int i = 0; i < n; ++i) {
         double bd = probs[i].error_bound;
         if (!(bd > 0.0) && h->err_bound > 0.0 && h->opt_slices <= 0) bd = h->err_bound;
         bound[i] = bd > 0.0 ? bd : 0.0;
-        if (bound[i] > 0.0) ++n_adapt;
+        if (bound[i] > 0.0) adapt_idx[i] = n_adapt++;
     }
-    // ---- statistics scratch: er, ec (int32); ssr, ssc, ca, rb (double) when adaptive
+    // ---- statistics scratch: er, ec (int32); ssr, ssc, ca, rb (double) when
+    // adaptive; the knob outputs of all adaptive problems contiguous at the end
     struct StatOff {
-        size_t er, ec, ssr, ssc, ca, rb, out;
+        size_t er, ec, ssr, ssc, ca, rb;
     };
     std::vector<StatOff> so(n);
     size_t total = 0;
     for (int i = 0; i < n; ++i) {
         const ozgb_problem &pb = probs[i];
+        so[i] = StatOff{};
         so[i].er = total;
         total += align256(sizeof(int32_t) * pb.M);
         so[i].ec = total;
@@ -418,16 +470,43 @@ ozgb_status enqueue_grouped(ozgb_handle h, ozgb_problem *probs, int n, int mode,
             total += align256(sizeof(double) * pb.K);
             so[i].rb = total;
             total += align256(sizeof(double) * pb.K);
-            so[i].out = total;
-            total += 256;
         }
     }
+    const size_t knob_off = total;
+    total += align256(sizeof(KnobStats) * (n_adapt + 1));
     if (!h->gstat.ensure(total)) return fail(h, OZGB_ERR_ALLOC, "grouped statistics buffer");
+    // job tables of both halves (phase 2: two split jobs per problem)
+    const size_t tab_bytes = align256(sizeof(StageJob) * 4 * n) + align256(sizeof(int) * (4 * n + 1)) +
+                             align256(sizeof(KnobJob) * (n_adapt + 1)) + align256(sizeof(StageJob) * 2 * n) +
+                             align256(sizeof(int) * (2 * n + 1));
+    if (!h->gtab.ensure(tab_bytes)) return fail(h, OZGB_ERR_ALLOC, "grouped table buffer");
+    if (n_adapt > 0 && h->knob_host_n < static_cast<size_t>(n_adapt)) {
+        if (h->knob_host) cudaFreeHost(h->knob_host);
+        h->knob_host = nullptr;
+        h->knob_host_n = 0;
+        if (cudaMallocHost(&h->knob_host, sizeof(KnobStats) * n_adapt) != cudaSuccess)
+            return fail(h, OZGB_ERR_ALLOC, "pinned knob buffer");
+        h->knob_host_n = n_adapt;
+    }
     uint8_t *gs = static_cast<uint8_t *>(h->gstat.p);
     auto at = [&](size_t off) { return gs + off; };
+    KnobStats *knob_dev = reinterpret_cast<KnobStats *>(at(knob_off));
 
-    // ---- stage (a) jobs
+    // ---- phase 1: stage (a) and the knob statistics
+    std::vector<long long> key1 = {n, mode, reinterpret_cast<long long>(gs), reinterpret_cast<long long>(h->gtab.p),
+                                   reinterpret_cast<long long>(h->knob_host)};
+    for (int i = 0; i < n; ++i) {
+        const ozgb_problem &pb = probs[i];
+        key1.insert(key1.end(), {pb.M, pb.N, pb.K, reinterpret_cast<long long>(pb.A), pb.lda,
+                                 reinterpret_cast<long long>(pb.B), pb.ldb, bound[i] > 0.0 ? 1 : 0});
+    }
+    const bool replay1 = graph && h->gexec1 && h->gkey1 == key1;
+    size_t toff = 0;
     JobList ja;
+    std::vector<KnobJob> kj;
+    const StageJob *dja = nullptr;
+    const int *dba = nullptr;
+    const KnobJob *dkj = nullptr;
     for (int i = 0; i < n; ++i) {
         const ozgb_problem &pb = probs[i];
         const bool ad = bound[i] > 0.0;
@@ -450,44 +529,44 @@ ozgb_status enqueue_grouped(ozgb_handle h, ozgb_problem *probs, int n, int mode,
             j.kind = JOB_ROWMAX, j.X = pb.B, j.ld = pb.ldb, j.rows = pb.K, j.cols = pb.N;
             j.ss_out = reinterpret_cast<double *>(at(so[i].rb));
             ja.add(j);
+            kj.push_back(KnobJob{reinterpret_cast<int32_t *>(at(so[i].er)), reinterpret_cast<double *>(at(so[i].ssr)),
+                                 pb.M, reinterpret_cast<int32_t *>(at(so[i].ec)),
+                                 reinterpret_cast<double *>(at(so[i].ssc)), pb.N,
+                                 reinterpret_cast<double *>(at(so[i].ca)), reinterpret_cast<double *>(at(so[i].rb)),
+                                 pb.K, reinterpret_cast<double *>(knob_dev + adapt_idx[i])});
         }
     }
     ja.block0.push_back(ja.total);
-    std::vector<KnobJob> kj;
-    for (int i = 0; i < n; ++i)
-        if (bound[i] > 0.0)
-            kj.push_back(KnobJob{reinterpret_cast<int32_t *>(at(so[i].er)), reinterpret_cast<double *>(at(so[i].ssr)),
-                                 probs[i].M, reinterpret_cast<int32_t *>(at(so[i].ec)),
-                                 reinterpret_cast<double *>(at(so[i].ssc)), probs[i].N,
-                                 reinterpret_cast<double *>(at(so[i].ca)), reinterpret_cast<double *>(at(so[i].rb)),
-                                 probs[i].K, reinterpret_cast<double *>(at(so[i].out))});
-    size_t tab_bytes = align256(sizeof(StageJob) * ja.jobs.size()) + align256(sizeof(int) * ja.block0.size()) +
-                       align256(sizeof(KnobJob) * (kj.size() + 1));
-    // generous bound for the phase-2 tables (two split jobs and one group entry per problem)
-    tab_bytes += align256(sizeof(StageJob) * 2 * n) + align256(sizeof(int) * (2 * n + 1));
-    if (!h->gtab.ensure(tab_bytes)) return fail(h, OZGB_ERR_ALLOC, "grouped table buffer");
-    size_t toff = 0;
-    cudaMemsetAsync(gs, 0, total, st);  // column maxima and sums are accumulated atomically
-    const StageJob *dja = put_table(h, ja.jobs, &toff, st);
-    const int *dba = put_table(h, ja.block0, &toff, st);
-    if (h->profiling) cudaEventRecord(h->ev[0], st);
-    launch_stage_jobs(dja, dba, static_cast<int>(ja.jobs.size()), ja.total, st);
-    h->launches += 1;
-    if (h->profiling) cudaEventRecord(h->ev[1], st);
+    if (!replay1) {
+        dja = put_table(h, ja.jobs, &toff, st);
+        dba = put_table(h, ja.block0, &toff, st);
+        if (!kj.empty()) dkj = put_table(h, kj, &toff, st);
+    }
+    const size_t toff2 = align256(sizeof(StageJob) * 4 * n) + align256(sizeof(int) * (4 * n + 1)) +
+                         align256(sizeof(KnobJob) * (n_adapt + 1));
+    if (prof) cudaEventRecord(h->ev[0], st);
+    ozgb_status rc = run_phase(h, graph, key1, &h->gkey1, &h->gexec1, st, [&](cudaStream_t s) -> ozgb_status {
+        // column maxima and sums are accumulated atomically: start from zero
+        cudaMemsetAsync(gs, 0, total, s);
+        launch_stage_jobs(dja, dba, static_cast<int>(ja.jobs.size()), ja.total, s);
+        if (n_adapt > 0) {
+            launch_knob_grouped(dkj, n_adapt, s);
+            cudaMemcpyAsync(h->knob_host, knob_dev, sizeof(KnobStats) * n_adapt, cudaMemcpyDeviceToHost, s);
+        }
+        return OZGB_OK;
+    });
+    if (rc) return rc;
+    h->launches += 1 + (n_adapt > 0 ? 1 : 0);
+    if (prof) cudaEventRecord(h->ev[1], st);
 
-    // ---- precision knob: one grouped reduction, one read-back
+    // ---- precision knob: slice counts from the read-back statistics
     std::vector<int> s_pick(n, 0);
-    if (!kj.empty()) {
-        const KnobJob *dkj = put_table(h, kj, &toff, st);
-        launch_knob_grouped(dkj, static_cast<int>(kj.size()), st);
-        h->launches += 1;
-        std::vector<KnobStats> ks(n);
-        for (int i = 0; i < n; ++i)
-            if (bound[i] > 0.0) cudaMemcpyAsync(&ks[i], at(so[i].out), sizeof(KnobStats), cudaMemcpyDeviceToHost, st);
+    if (n_adapt > 0) {
         const cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return cuda_fail(h, e, "grouped statistics readback");
         for (int i = 0; i < n; ++i)
-            if (bound[i] > 0.0) s_pick[i] = choose_slices_stats(ks[i], probs[i].K, 7, bound[i], 2, 16, nullptr);
+            if (bound[i] > 0.0)
+                s_pick[i] = choose_slices_stats(h->knob_host[adapt_idx[i]], probs[i].K, 7, bound[i], 2, 16, nullptr);
     }
 
     // ---- plans
@@ -504,7 +583,7 @@ ozgb_status enqueue_grouped(ozgb_handle h, ozgb_problem *probs, int n, int mode,
             return fail(h, OZGB_ERR_UNSUPPORTED, "problem " + std::to_string(i) + ": " + why);
         probs[i].slices_used = plans[i].cfg.s;
     }
-    // ---- stage (b): slice planes of every problem, one launch
+    // ---- phase 2: stage (b) for every problem (one launch) and the GEMMs
     std::vector<size_t> a_off(n), b_off(n);
     size_t sl_total = 0;
     for (int i = 0; i < n; ++i) {
@@ -515,6 +594,22 @@ ozgb_status enqueue_grouped(ozgb_handle h, ozgb_problem *probs, int n, int mode,
     }
     if (!h->gslice.ensure(sl_total)) return fail(h, OZGB_ERR_ALLOC, "grouped slice buffer");
     uint8_t *gsl = static_cast<uint8_t *>(h->gslice.p);
+    if (!h->ev_fork) {
+        bool okc = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) == cudaSuccess;
+        for (int a = 0; okc && a < ozgb_context::kAux; ++a)
+            okc = cudaStreamCreateWithFlags(&h->aux[a], cudaStreamNonBlocking) == cudaSuccess &&
+                  cudaEventCreateWithFlags(&h->ev_join[a], cudaEventDisableTiming) == cudaSuccess;
+        if (!okc) return cuda_fail(h, cudaGetLastError(), "auxiliary streams");
+    }
+    std::vector<long long> key2 = key1;
+    key2.insert(key2.end(), {reinterpret_cast<long long>(gsl), reinterpret_cast<long long>(h->err.p),
+                             static_cast<long long>(h->timeout_ns)});
+    for (int i = 0; i < n; ++i) {
+        const Plan &p = plans[i];
+        key2.insert(key2.end(), {reinterpret_cast<long long>(probs[i].C), probs[i].ldc, p.cfg.b, p.cfg.s, p.cfg.J,
+                                 p.cfg.rounding, p.BN, p.KC, p.stages, p.G});
+    }
+    const bool replay2 = graph && h->gexec2 && h->gkey2 == key2;
     JobList jb;
     for (int i = 0; i < n; ++i) {
         const ozgb_problem &pb = probs[i];
@@ -532,22 +627,14 @@ ozgb_status enqueue_grouped(ozgb_handle h, ozgb_problem *probs, int n, int mode,
         jb.add(j);
     }
     jb.block0.push_back(jb.total);
-    const StageJob *djb = put_table(h, jb.jobs, &toff, st);
-    const int *dbb = put_table(h, jb.block0, &toff, st);
-    launch_stage_jobs(djb, dbb, static_cast<int>(jb.jobs.size()), jb.total, st);
-    h->launches += 1;
-    if (h->profiling) cudaEventRecord(h->ev[2], st);
-
-    // ---- stage (c)+(d): one persistent launch per problem; the launches are spread
-    // (largest first) over auxiliary streams forked from st, so that problems that
-    // fill few SMs run side by side
-    if (!h->ev_fork) {
-        bool okc = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) == cudaSuccess;
-        for (int a = 0; okc && a < ozgb_context::kAux; ++a)
-            okc = cudaStreamCreateWithFlags(&h->aux[a], cudaStreamNonBlocking) == cudaSuccess &&
-                  cudaEventCreateWithFlags(&h->ev_join[a], cudaEventDisableTiming) == cudaSuccess;
-        if (!okc) return cuda_fail(h, cudaGetLastError(), "auxiliary streams");
+    const StageJob *djb = nullptr;
+    const int *dbb = nullptr;
+    if (!replay2) {
+        toff = toff2;
+        djb = put_table(h, jb.jobs, &toff, st);
+        dbb = put_table(h, jb.block0, &toff, st);
     }
+    // the GEMMs, largest first, spread over the auxiliary streams
     std::vector<int> order(n);
     for (int i = 0; i < n; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
@@ -555,35 +642,40 @@ ozgb_status enqueue_grouped(ozgb_handle h, ozgb_problem *probs, int n, int mode,
                static_cast<double>(plans[y].tiles_m) * plans[y].tiles_n * plans[y].n_kc * plans[y].pairs;
     });
     const int n_aux = std::min(n, static_cast<int>(ozgb_context::kAux));
-    cudaEventRecord(h->ev_fork, st);
-    for (int a = 0; a < n_aux; ++a) cudaStreamWaitEvent(h->aux[a], h->ev_fork, 0);
-    for (int r = 0; r < n; ++r) {
-        const int k = order[r];
-        const Plan &p = plans[k];
-        GemmArgs g;
-        gemm_args_from_plan(&g, p, p.cfg.rounding, static_cast<int *>(h->err.p), h->timeout_ns);
-        g.a_tiles = reinterpret_cast<const uint16_t *>(gsl + a_off[k]);
-        g.b_tiles = reinterpret_cast<const uint16_t *>(gsl + b_off[k]);
-        g.er = reinterpret_cast<const int32_t *>(at(so[k].er));
-        g.ec = reinterpret_cast<const int32_t *>(at(so[k].ec));
-        g.c = probs[k].C;
-        g.ldc = probs[k].ldc;
-        g.M = probs[k].M;
-        g.N = probs[k].N;
-        g.n_kc = p.n_kc;
-        g.tiles_m = p.tiles_m;
-        g.tiles_n = p.tiles_n;
-        g.total_tiles = p.tiles_m * p.tiles_n;
-        p.fn(g, g.total_tiles, p.smem, h->aux[r % n_aux]);
-        h->launches += 1;
-    }
-    for (int a = 0; a < n_aux; ++a) {
-        cudaEventRecord(h->ev_join[a], h->aux[a]);
-        cudaStreamWaitEvent(st, h->ev_join[a], 0);
-    }
-    const cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_fail(h, e, "grouped slice-pair GEMM launches");
-    if (h->profiling) {
+    rc = run_phase(h, graph, key2, &h->gkey2, &h->gexec2, st, [&](cudaStream_t s) -> ozgb_status {
+        launch_stage_jobs(djb, dbb, static_cast<int>(jb.jobs.size()), jb.total, s);
+        if (prof) cudaEventRecord(h->ev[2], s);
+        cudaEventRecord(h->ev_fork, s);
+        for (int a = 0; a < n_aux; ++a) cudaStreamWaitEvent(h->aux[a], h->ev_fork, 0);
+        for (int r = 0; r < n; ++r) {
+            const int k = order[r];
+            const Plan &p = plans[k];
+            GemmArgs g;
+            gemm_args_from_plan(&g, p, p.cfg.rounding, static_cast<int *>(h->err.p), h->timeout_ns);
+            g.a_tiles = reinterpret_cast<const uint16_t *>(gsl + a_off[k]);
+            g.b_tiles = reinterpret_cast<const uint16_t *>(gsl + b_off[k]);
+            g.er = reinterpret_cast<const int32_t *>(at(so[k].er));
+            g.ec = reinterpret_cast<const int32_t *>(at(so[k].ec));
+            g.c = probs[k].C;
+            g.ldc = probs[k].ldc;
+            g.M = probs[k].M;
+            g.N = probs[k].N;
+            g.n_kc = p.n_kc;
+            g.tiles_m = p.tiles_m;
+            g.tiles_n = p.tiles_n;
+            g.total_tiles = p.tiles_m * p.tiles_n;
+            p.fn(g, g.total_tiles, p.smem, h->aux[r % n_aux]);
+        }
+        for (int a = 0; a < n_aux; ++a) {
+            cudaEventRecord(h->ev_join[a], h->aux[a]);
+            cudaStreamWaitEvent(s, h->ev_join[a], 0);
+        }
+        const cudaError_t e = cudaGetLastError();
+        return e == cudaSuccess ? OZGB_OK : cuda_fail(h, e, "grouped slice-pair GEMM launches");
+    });
+    if (rc) return rc;
+    h->launches += 1 + n;
+    if (prof) {
         cudaEventRecord(h->ev[3], st);
         h->ev_recorded = true;
     }
@@ -622,6 +714,12 @@ ozgb_status ozgb_release(ozgb_handle h) {
     for (DevBuf *b : {&h->a, &h->b, &h->c, &h->at, &h->bt, &h->er, &h->ec, &h->ssr, &h->ssc, &h->raw, &h->knob, &h->kca,
                       &h->krb, &h->ktmp, &h->gstat, &h->gslice, &h->gtab})
         b->release();
+    // captured grouped graphs refer to the released buffers
+    if (h->gexec1) cudaGraphExecDestroy(h->gexec1);
+    if (h->gexec2) cudaGraphExecDestroy(h->gexec2);
+    h->gexec1 = h->gexec2 = nullptr;
+    h->gkey1.clear();
+    h->gkey2.clear();
     h->setup_done = false;
     return OZGB_OK;
 }
@@ -640,6 +738,7 @@ ozgb_status ozgb_destroy(ozgb_handle h) {
             if (h->ev_join[i]) cudaEventDestroy(h->ev_join[i]);
         }
         if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+        if (h->knob_host) cudaFreeHost(h->knob_host);
     }
     delete h;
     return OZGB_OK;
