@@ -183,6 +183,21 @@ ozgb_status ozgb_selftest_timeout(ozgb_handle h, double timeout_ms);
 ozgb_status ozgb_convert_paired_i64_to_double(const int64_t *C, double *result, int M, int N, int K,
                                               int num_splits, int bits_per_slice);
 
+/* Autotuner (no reference counterpart; the reference fixes its tiling per
+ * shape).  Times up to max_candidates feasible plans (tile width, K chunk,
+ * number of bin blocks, pipeline depth) of the slice-pair GEMM for an M x N x K
+ * product with `bits`, `slices`, `bins` (0 = slices, the triangular set) on
+ * this handle's device, with pseudo-random operands, and records the fastest in
+ * a process-wide table keyed by (bits, slices, bins, rounding, ceil(log2) of
+ * M, N, K).  Later calls of any handle with a matching configuration use it.
+ * Writes the winner to *best (may be NULL).  Allocates device memory. */
+ozgb_status ozgb_autotune(ozgb_handle h, int M, int N, int K, int bits, int slices, int bins, int max_candidates,
+                          ozgb_config *best);
+/* Number of entries in the tuning table; clearing it restores the planner's
+ * cost-model choices. */
+int ozgb_tuning_entries(void);
+void ozgb_tuning_clear(void);
+
 /* Host-only planning query (no device needed): the kernel configuration the
  * library would use for an M x N x K product with `bits`, `slices`, `bins`. */
 int ozgb_plan_query(int M, int N, int K, int bits, int slices, int bins, ozgb_config *out);

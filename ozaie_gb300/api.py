@@ -146,6 +146,13 @@ class Handle:
         self._check(self._L.ozgb_stage_times(self._h, t, 4))
         return {"exponents": t[0], "split": t[1], "gemm": t[2], "total": t[3]}
 
+    def autotune(self, M, N, K, bits=7, slices=9, bins=0, max_candidates=64):
+        """Times candidate plans for this configuration and records the fastest
+        in the process-wide tuning table; returns its configuration."""
+        c = OzgbConfig()
+        self._check(self._L.ozgb_autotune(self._h, M, N, K, bits, slices, bins, max_candidates, ctypes.byref(c)))
+        return c.as_dict()
+
     def launch_count(self):
         n = ctypes.c_longlong()
         self._check(self._L.ozgb_launch_count(self._h, ctypes.byref(n)))
@@ -197,6 +204,14 @@ def q_words_to_int(q):
             v -= 1 << 128
         out[i] = v
     return out.reshape(q.shape[:-1])
+
+
+def tuning_entries():
+    return load().ozgb_tuning_entries()
+
+
+def tuning_clear():
+    load().ozgb_tuning_clear()
 
 
 def plan_query(M, N, K, bits, slices, bins):

@@ -352,21 +352,6 @@ ozgb_status check_device_error(ozgb_handle h, cudaStream_t st) {
 // ------------------------------------------------------------ grouped calls
 size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
 
-// Plan fields that the GEMM kernel takes from its launch arguments: problems
-// whose plans agree on all of them share one grouped launch.
-bool same_launch_class(const Plan &x, const Plan &y) {
-    if (x.fn != y.fn || x.cfg.b != y.cfg.b || x.cfg.s != y.cfg.s || x.cfg.J != y.cfg.J ||
-        x.cfg.rounding != y.cfg.rounding || x.KC != y.KC || x.stages != y.stages || x.stage_bytes != y.stage_bytes ||
-        x.a_block_bytes != y.a_block_bytes || x.b_block_bytes != y.b_block_bytes || x.pad_lo != y.pad_lo ||
-        x.b_region_bytes != y.b_region_bytes || x.tmem_cols != y.tmem_cols || x.smem != y.smem || x.G != y.G)
-        return false;
-    for (int i = 0; i < x.G; ++i)
-        if (x.blk_lo[i] != y.blk_lo[i] || x.blk_nb[i] != y.blk_nb[i] || x.blk_p0[i] != y.blk_p0[i] ||
-            x.blk_p1[i] != y.blk_p1[i] || x.blk_period[i] != y.blk_period[i] || x.blk_off[i] != y.blk_off[i])
-            return false;
-    return true;
-}
-
 // Uploads a host table into the grouped-table buffer at byte offset *off.
 template <typename T>
 const T *put_table(ozgb_handle h, const std::vector<T> &v, size_t *off, cudaStream_t st) {
@@ -1043,6 +1028,100 @@ ozgb_status ozgb_convert_paired_i64_to_double(const int64_t *C, double *result, 
 }
 
 // Host-only planning queries (no device needed): used by tests and tools.
+ozgb_status ozgb_autotune(ozgb_handle h, int M, int N, int K, int bits, int slices, int bins, int max_candidates,
+                          ozgb_config *best) {
+    if (!h) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (M < 1 || N < 1 || K < 1) return fail(h, OZGB_ERR_DIMS, "dimensions must be positive");
+    ozgb_status rc = ensure_device(h);
+    if (rc) return rc;
+    OzConfig cfg;
+    cfg.b = bits;
+    cfg.s = slices;
+    cfg.J = bins > 0 ? bins : slices;
+    cfg.rounding = OUT_RN;
+    const std::vector<PlanHints> cands = plan_candidates(M, N, K, cfg, max_candidates > 0 ? max_candidates : 64);
+    if (cands.empty()) return fail(h, OZGB_ERR_UNSUPPORTED, "no feasible plan for this configuration");
+    cudaStream_t st = h->stream;
+    if (!h->a.ensure(sizeof(double) * M * K) || !h->b.ensure(sizeof(double) * K * N) ||
+        !h->c.ensure(sizeof(double) * M * N) || !h->er.ensure(sizeof(int32_t) * M) || !h->ec.ensure(sizeof(int32_t) * N))
+        return fail(h, OZGB_ERR_ALLOC, "autotune buffers");
+    const double *dA = static_cast<double *>(h->a.p), *dB = static_cast<double *>(h->b.p);
+    launch_fill_random(static_cast<double *>(h->a.p), static_cast<size_t>(M) * K, 1, st);
+    launch_fill_random(static_cast<double *>(h->b.p), static_cast<size_t>(K) * N, 2, st);
+    cudaMemsetAsync(h->ec.p, 0, sizeof(int32_t) * N, st);
+    launch_rowmax(dA, K, M, K, static_cast<int32_t *>(h->er.p), nullptr, st);
+    launch_colmax(dB, N, K, N, static_cast<int32_t *>(h->ec.p), nullptr, st);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best_ms = 0.0f;
+    int best_i = -1;
+    Plan best_plan;
+    for (size_t i = 0; i < cands.size(); ++i) {
+        Plan p;
+        std::string why;
+        if (!make_plan(M, N, K, cfg, &p, &why, 0, 1 << 30, &cands[i])) continue;
+        if (!h->at.ensure(p.a_elems * 2) || !h->bt.ensure(p.b_elems * 2)) continue;
+        uint16_t *at = static_cast<uint16_t *>(h->at.p), *bt = static_cast<uint16_t *>(h->bt.p);
+        launch_split_a(dA, K, M, K, static_cast<int32_t *>(h->er.p), p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.Mp, at, st);
+        launch_split_b(dB, N, K, N, static_cast<int32_t *>(h->ec.p), p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.BN, p.Np, bt, st);
+        GemmArgs g;
+        gemm_args_from_plan(&g, p, OUT_RN, static_cast<int *>(h->err.p), h->timeout_ns);
+        g.a_tiles = at;
+        g.b_tiles = bt;
+        g.er = static_cast<int32_t *>(h->er.p);
+        g.ec = static_cast<int32_t *>(h->ec.p);
+        g.c = static_cast<double *>(h->c.p);
+        g.ldc = N;
+        g.M = M;
+        g.N = N;
+        g.n_kc = p.n_kc;
+        g.tiles_m = p.tiles_m;
+        g.tiles_n = p.tiles_n;
+        g.total_tiles = p.tiles_m * p.tiles_n;
+        p.fn(g, g.total_tiles, p.smem, st);  // warm-up
+        float t[3];
+        for (float &ti : t) {
+            cudaEventRecord(e0, st);
+            p.fn(g, g.total_tiles, p.smem, st);
+            cudaEventRecord(e1, st);
+            cudaEventSynchronize(e1);
+            cudaEventElapsedTime(&ti, e0, e1);
+        }
+        h->launches += 6;
+        if ((rc = check_device_error(h, st))) break;
+        std::sort(t, t + 3);
+        if (best_i < 0 || t[1] < best_ms) {
+            best_ms = t[1];
+            best_i = static_cast<int>(i);
+            best_plan = p;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if (best_i < 0) return fail(h, OZGB_ERR_UNSUPPORTED, "no candidate plan ran");
+    tune_store(M, N, K, cfg, cands[best_i]);
+    if (best) {
+        best->bits = best_plan.cfg.b;
+        best->slices = best_plan.cfg.s;
+        best->bins = best_plan.cfg.J;
+        best->rounding = best_plan.cfg.rounding;
+        best->tile_n = best_plan.BN;
+        best->k_chunk = best_plan.KC;
+        best->stages = best_plan.stages;
+        best->drain_chunks = best_plan.min_period;
+        best->acc_words = best_plan.W;
+        best->pairs = best_plan.pairs;
+        fill_blocks(best_plan, best);
+    }
+    return OZGB_OK;
+}
+
+int ozgb_tuning_entries(void) { return tune_count(); }
+void ozgb_tuning_clear(void) { tune_clear(); }
+
 int ozgb_plan_query(int M, int N, int K, int bits, int slices, int bins, ozgb_config *out) {
     OzConfig c;
     c.b = bits;

@@ -137,5 +137,7 @@ void stage_grid(const StageJob &j, int *gx, int *gy);
 // block0[n_jobs] = total), and the knob reduction of n problems.
 void launch_stage_jobs(const StageJob *jobs, const int *block0, int n_jobs, int total_blocks, void *stream);
 void launch_knob_grouped(const KnobJob *jobs, int n, void *stream);
+// Pseudo-random doubles in [-1, 1) for timing runs.
+void launch_fill_random(double *x, size_t n, unsigned long long seed, void *stream);
 
 }  // namespace ozgb

@@ -4,6 +4,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 namespace ozgb {
@@ -42,7 +45,47 @@ void reference_table(int K, int mode, int *b, int *d) {
     }
 }
 
-bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string *err, int bin_lo, int bin_hi) {
+namespace {
+using TuneKey = std::tuple<int, int, int, int, int, int, int>;
+std::mutex g_tune_mu;
+std::map<TuneKey, PlanHints> g_tune;
+
+int ceil_log2(int x) {
+    int l = 0;
+    while ((1L << l) < x) ++l;
+    return l;
+}
+TuneKey tune_key(int M, int N, int K, const OzConfig &cfg) {
+    return TuneKey{cfg.b, cfg.s, cfg.J, cfg.rounding, ceil_log2(M), ceil_log2(N), ceil_log2(K)};
+}
+}  // namespace
+
+void tune_store(int M, int N, int K, const OzConfig &cfg, const PlanHints &h) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[tune_key(M, N, K, cfg)] = h;
+}
+bool tune_lookup(int M, int N, int K, const OzConfig &cfg, PlanHints *h) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(tune_key(M, N, K, cfg));
+    if (it == g_tune.end()) return false;
+    *h = it->second;
+    return true;
+}
+void tune_clear() {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune.clear();
+}
+int tune_count() {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    return static_cast<int>(g_tune.size());
+}
+
+bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string *err, int bin_lo, int bin_hi,
+               const PlanHints *hints) {
+    PlanHints tuned;
+    if (!hints && bin_lo <= 0 && bin_hi >= cfg.J - 1 && tune_lookup(M, N, K, cfg, &tuned)) hints = &tuned;
+    const PlanHints none;
+    const PlanHints &hint = hints ? *hints : none;
     Plan p;
     p.cfg = cfg;
     const int b = cfg.b, s = cfg.s, J = cfg.J;
@@ -94,6 +137,7 @@ bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string 
     const Variant *chosen = nullptr;
     for (const Variant &v : kVariants) {
         if (v.KC != 32) continue;
+        if (hint.BN && v.BN != hint.BN) continue;
         if (v.BN * J > 512) continue;
         if (32 * v.W < bits) continue;
         chosen = &v;
@@ -137,8 +181,10 @@ bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string 
                 }
             }
     int gbest = -1;
-    for (int g = 1; g <= max_groups; ++g)
+    for (int g = 1; g <= max_groups; ++g) {
+        if (hint.groups && g != hint.groups) continue;
         if (best[g][nbins] < INF && (gbest < 0 || best[g][nbins] < best[gbest][nbins] - 1e-9)) gbest = g;
+    }
     if (gbest < 0) {
         *err = "bins do not fit " + std::to_string(max_groups) + " blocks of at most 256 columns";
         return false;
@@ -170,7 +216,7 @@ bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string 
     const size_t budget = kSmemLimit - kSmemReserve;
     const int kc_opts[2] = {32, 16};
     const char *env_kc = std::getenv("OZGB_KC");  // tuning override
-    const int force_kc = env_kc ? std::atoi(env_kc) : 0;
+    const int force_kc = hint.KC ? hint.KC : (env_kc ? std::atoi(env_kc) : 0);
     auto stage_of = [&](int kc) {
         return static_cast<size_t>(s) * BM * kc * 2 + static_cast<size_t>(p.pad_lo + s + p.pad_hi) * p.BN * kc * 2;
     };
@@ -183,6 +229,7 @@ bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string 
         if (st >= 2) {
             p.KC = kc;
             p.stages = static_cast<int>(std::min<size_t>(st, 8));
+            if (hint.stages >= 2) p.stages = std::min(p.stages, hint.stages);
             break;
         }
     }
@@ -238,6 +285,45 @@ bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string 
     p.smem = static_cast<size_t>(p.stages) * p.stage_bytes + kCtrlBytes;
     *out = p;
     return true;
+}
+
+std::vector<PlanHints> plan_candidates(int M, int N, int K, const OzConfig &cfg, int max_n) {
+    std::vector<PlanHints> out;
+    std::vector<Plan> plans;
+    auto same = [](const Plan &x, const Plan &y) {
+        if (x.BN != y.BN || x.KC != y.KC || x.G != y.G || x.stages != y.stages) return false;
+        for (int i = 0; i < x.G; ++i)
+            if (x.blk_lo[i] != y.blk_lo[i] || x.blk_nb[i] != y.blk_nb[i]) return false;
+        return true;
+    };
+    auto try_add = [&](const PlanHints &h) {
+        if (static_cast<int>(out.size()) >= max_n) return;
+        Plan p;
+        std::string why;
+        if (!make_plan(M, N, K, cfg, &p, &why, 0, 1 << 30, &h)) return;
+        for (const Plan &q : plans)
+            if (same(p, q)) return;
+        PlanHints exact = h;
+        exact.BN = p.BN;
+        exact.KC = p.KC;
+        exact.groups = p.G;
+        exact.stages = p.stages;
+        plans.push_back(p);
+        out.push_back(exact);
+    };
+    try_add(PlanHints{});  // the cost-model choice
+    const int bns[] = {128, 64, 48, 32, 16};
+    const int kcs[] = {32, 16};
+    for (int bn : bns)
+        for (int kc : kcs)
+            for (int g = 1; g <= kMaxGroups; ++g) {
+                PlanHints h;
+                h.BN = bn;
+                h.KC = kc;
+                h.groups = g;
+                try_add(h);
+            }
+    return out;
 }
 
 double knob_estimate(const KnobStats &k, int K, int b, int s) {

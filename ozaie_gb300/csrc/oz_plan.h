@@ -4,6 +4,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <string>
+#include <vector>
 
 #include "oz_internal.h"
 
@@ -39,11 +40,30 @@ inline int pairs_in_bin(int j, int s) {
     return hi >= lo ? hi - lo + 1 : 0;
 }
 
+// Choices a plan may be forced to (0 = the planner's own choice): tile width BN,
+// K chunk, number of bin blocks (the cheapest partition with exactly that many),
+// pipeline stages.  The autotuner times candidates built from these.
+struct PlanHints {
+    int BN = 0, KC = 0, groups = 0, stages = 0;
+};
+
 // Builds the plan for bins [bin_lo, bin_hi] of the pair set (the full set of
 // bins normally; a sub-range for parity dumps).  Returns false with a message
-// when the configuration is outside the limits of the exact accumulation.
+// when the configuration is outside the limits of the exact accumulation.  With
+// no hints, a tuned entry for the problem's size class (tune_store) is used when
+// one exists.
 bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string *err, int bin_lo = 0,
-               int bin_hi = 1 << 30);
+               int bin_hi = 1 << 30, const PlanHints *hints = nullptr);
+
+// Distinct feasible plans for the autotuner (at most max_n), the untuned plan first.
+std::vector<PlanHints> plan_candidates(int M, int N, int K, const OzConfig &cfg, int max_n);
+
+// Process-wide tuning table: the best hints per (bits, slices, bins, rounding,
+// size class), the size class being ceil(log2) of M, N and K.
+void tune_store(int M, int N, int K, const OzConfig &cfg, const PlanHints &h);
+bool tune_lookup(int M, int N, int K, const OzConfig &cfg, PlanHints *h);
+void tune_clear();
+int tune_count();
 
 // The reference's (b, d) tables, include/oz_aie.h:60-80, indexed by log2 K.
 void reference_table(int K, int mode, int *b, int *d);

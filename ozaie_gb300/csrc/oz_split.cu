@@ -320,6 +320,23 @@ __global__ void __launch_bounds__(kStageThreads) k_stage_jobs(const StageJob *__
     }
 }
 
+// Pseudo-random doubles in [-1, 1) (splitmix64 of the index): inputs for the
+// autotuner's timing runs, whose speed does not depend on the values.
+__global__ void k_fill_random(double *__restrict__ x, size_t n, unsigned long long seed) {
+    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        unsigned long long z = seed + 0x9E3779B97F4A7C15ull * (i + 1);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        x[i] = static_cast<double>(z >> 11) * 0x1.0p-52 - 1.0;
+    }
+}
+
+void launch_fill_random(double *x, size_t n, unsigned long long seed, void *stream) {
+    if (n) k_fill_random<<<4 * 152, 256, 0, static_cast<cudaStream_t>(stream)>>>(x, n, seed);
+}
+
 void stage_grid(const StageJob &j, int *gx, int *gy) {
     switch (j.kind) {
         case JOB_ROWMAX:

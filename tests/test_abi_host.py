@@ -209,3 +209,12 @@ def test_cmake_use_ozaie_helper(ozlib, tmp_path):
     subprocess.check_call(["cmake", "--build", str(b)], env=env, stdout=subprocess.DEVNULL)
     rc = subprocess.run([str(b / "oztest")], capture_output=True, timeout=120)
     assert rc.returncode == (0 if HAVE_GPU else 2)
+
+
+def test_tuning_table_starts_empty_and_clears(ozlib):
+    from ozaie_gb300 import api
+    api.tuning_clear()
+    assert api.tuning_entries() == 0
+    # a host-only plan query never consults or fills the table
+    assert ozlib.plan_query(1024, 1024, 1024, 7, 9, 9) is not None
+    assert api.tuning_entries() == 0
