@@ -200,6 +200,28 @@ bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string 
             i = k;
         }
     }
+    if (hint.groups && hint.sizes[0] > 0) {
+        // explicit block sizes: contiguous, covering the bins, each at most 256 columns
+        int at = B0;
+        double cost = 0.0;
+        for (int g = 0; g < hint.groups; ++g) {
+            const int nb = hint.sizes[g];
+            if (nb < 1 || nb > maxb || at + nb - 1 > B1) {
+                *err = "hinted bin blocks do not fit";
+                return false;
+            }
+            p.blk_lo[g] = at;
+            p.blk_nb[g] = nb;
+            cost += blk_cost(at, at + nb - 1);
+            at += nb;
+        }
+        if (at != B1 + 1) {
+            *err = "hinted bin blocks do not cover the bins";
+            return false;
+        }
+        p.G = hint.groups;
+        p.model_cycles_per_kstep = cost;
+    }
     p.pad_lo = 0;
     p.pad_hi = 0;
     p.mma_per_kstep = 0;
@@ -297,7 +319,6 @@ std::vector<PlanHints> plan_candidates(int M, int N, int K, const OzConfig &cfg,
         return true;
     };
     auto try_add = [&](const PlanHints &h) {
-        if (static_cast<int>(out.size()) >= max_n) return;
         Plan p;
         std::string why;
         if (!make_plan(M, N, K, cfg, &p, &why, 0, 1 << 30, &h)) return;
@@ -308,12 +329,27 @@ std::vector<PlanHints> plan_candidates(int M, int N, int K, const OzConfig &cfg,
         exact.KC = p.KC;
         exact.groups = p.G;
         exact.stages = p.stages;
+        for (int g = 0; g < kMaxGroups; ++g) exact.sizes[g] = g < p.G ? p.blk_nb[g] : 0;
         plans.push_back(p);
         out.push_back(exact);
     };
     try_add(PlanHints{});  // the cost-model choice
     const int bns[] = {128, 64, 48, 32, 16};
     const int kcs[] = {32, 16};
+    // explicit two-block splits of the bins first (they trade UMMA width for
+    // drain overlap, which the cost model does not see), then the cost model's
+    // best partition for each block count
+    for (int bn : bns)
+        for (int kc : kcs)
+            for (int cut = 1; cut < cfg.J; ++cut) {
+                PlanHints h;
+                h.BN = bn;
+                h.KC = kc;
+                h.groups = 2;
+                h.sizes[0] = cut;
+                h.sizes[1] = cfg.J - cut;
+                try_add(h);
+            }
     for (int bn : bns)
         for (int kc : kcs)
             for (int g = 1; g <= kMaxGroups; ++g) {
@@ -323,7 +359,23 @@ std::vector<PlanHints> plan_candidates(int M, int N, int K, const OzConfig &cfg,
                 h.groups = g;
                 try_add(h);
             }
-    return out;
+    // keep the candidates whose modelled UMMA cycles per output column are within
+    // 35 % of the best, cheapest first (the untuned plan stays first)
+    std::vector<double> score(plans.size());
+    double best = 1e300;
+    for (size_t i = 0; i < plans.size(); ++i) {
+        score[i] = plans[i].model_cycles_per_kstep / plans[i].BN;
+        best = std::min(best, score[i]);
+    }
+    std::vector<size_t> idx;
+    for (size_t i = 1; i < plans.size(); ++i)
+        if (score[i] <= 1.35 * best) idx.push_back(i);
+    std::stable_sort(idx.begin(), idx.end(), [&](size_t x, size_t y) { return score[x] < score[y]; });
+    std::vector<PlanHints> kept;
+    if (!out.empty()) kept.push_back(out[0]);
+    for (size_t i : idx)
+        if (static_cast<int>(kept.size()) < max_n) kept.push_back(out[i]);
+    return kept;
 }
 
 double knob_estimate(const KnobStats &k, int K, int b, int s) {

@@ -41,10 +41,12 @@ inline int pairs_in_bin(int j, int s) {
 }
 
 // Choices a plan may be forced to (0 = the planner's own choice): tile width BN,
-// K chunk, number of bin blocks (the cheapest partition with exactly that many),
-// pipeline stages.  The autotuner times candidates built from these.
+// K chunk, number of bin blocks (the cheapest partition with exactly that many,
+// or the explicit block sizes), pipeline stages.  The autotuner times
+// candidates built from these.
 struct PlanHints {
     int BN = 0, KC = 0, groups = 0, stages = 0;
+    int sizes[kMaxGroups] = {0};  // explicit bin-block sizes (groups of them), overriding the cost model
 };
 
 // Builds the plan for bins [bin_lo, bin_hi] of the pair set (the full set of
