@@ -200,6 +200,70 @@ bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string 
             i = k;
         }
     }
+    if (!hint.groups && !std::getenv("OZGB_GROUPS")) {
+        // Drain-aware choice among the cost model's best partition per block count
+        // and every two-block split.  A block drained after a chunk must be read out
+        // (about 0.1 SM cycles per value: 16 F2I conversions per cycle) before its
+        // next UMMA; the other blocks' UMMAs of that chunk and the next one cover
+        // the read-out, and what they do not cover stalls the tensor pipe once per
+        // drain period.  Modelled per 32-deep chunk.
+        auto period_of = [&](int lo, int nb) {
+            long kb = 1L << 40;
+            for (int j = lo; j < lo + nb; ++j)
+                kb = std::min(kb, static_cast<long>(std::floor(16777216.0 / (pairs_in_bin(j, s) * v2 * v2))));
+            return std::max(1L, kb / 32);
+        };
+        auto total_cost = [&](int G, const int *lo, const int *nb) {
+            double umma[kMaxGroups], all = 0.0;
+            for (int g = 0; g < G; ++g) {
+                umma[g] = 2.0 * blk_cost(lo[g], lo[g] + nb[g] - 1);
+                all += umma[g];
+            }
+            double stall = 0.0;
+            for (int g = 0; g < G; ++g) {
+                const double drain = 0.1 * nb[g] * p.BN * BM;
+                const double cover = 2.0 * (all - umma[g]);
+                stall += std::max(0.0, drain - cover) / static_cast<double>(period_of(lo[g], nb[g]));
+            }
+            return all + stall;
+        };
+        int cur_lo[kMaxGroups], cur_nb[kMaxGroups];
+        for (int g = 0; g < p.G; ++g) {
+            cur_lo[g] = p.blk_lo[g];
+            cur_nb[g] = p.blk_nb[g];
+        }
+        double best_total = total_cost(p.G, cur_lo, cur_nb);
+        auto consider = [&](int G, const int *lo, const int *nb) {
+            const double c = total_cost(G, lo, nb);
+            if (c < best_total - 1e-9) {
+                best_total = c;
+                p.G = G;
+                p.model_cycles_per_kstep = 0.0;
+                for (int g = 0; g < G; ++g) {
+                    p.blk_lo[g] = lo[g];
+                    p.blk_nb[g] = nb[g];
+                    p.model_cycles_per_kstep += blk_cost(lo[g], lo[g] + nb[g] - 1);
+                }
+            }
+        };
+        for (int g = 1; g <= max_groups; ++g) {
+            if (best[g][nbins] >= INF) continue;
+            int lo[kMaxGroups], nb[kMaxGroups];
+            int i = nbins;
+            for (int k = g; k >= 1; --k) {
+                const int f = from[k][i];
+                lo[k - 1] = B0 + f;
+                nb[k - 1] = i - f;
+                i = f;
+            }
+            consider(g, lo, nb);
+        }
+        for (int cut = 1; cut < nbins; ++cut) {
+            if (cut > maxb || nbins - cut > maxb) continue;
+            const int lo[2] = {B0, B0 + cut}, nb[2] = {cut, nbins - cut};
+            consider(2, lo, nb);
+        }
+    }
     if (hint.groups && hint.sizes[0] > 0) {
         // explicit block sizes: contiguous, covering the bins, each at most 256 columns
         int at = B0;
