@@ -177,6 +177,12 @@ ozgb_status ozgb_dump(ozgb_handle h, int M, int N, int K, const double *A, const
  * the given limit; returns OZGB_ERR_TIMEOUT when the bounded wait gave up and the
  * device stayed usable (tests the timeout path without faulting the GPU). */
 ozgb_status ozgb_selftest_timeout(ozgb_handle h, double timeout_ms);
+/* The reference's device output for A B (host arrays, the handle's profile and
+ * mode; triangular pair set): pairs[(row * N + col) * 2] = lo and [+1] = hi, the
+ * two int64 sums of ozaki_vectorized_sum_upshift (ozaki_base.cc:143-340) with
+ * Er + Ec in bits 51..62 of hi -- the buffer that ozAIE_DGEMM reads back before
+ * convert_paired_i64_to_double_matrix (include/oz_aie.h:342-346). */
+ozgb_status ozgb_dump_pairs(ozgb_handle h, int M, int N, int K, const double *A, const double *B, int64_t *pairs);
 
 /* Host helper kept from the reference: decodes the 2 x int64 per element wire
  * format (include/oz_aie.h:92-150), C[row*(2N) + 2col] = low, +1 = high. */

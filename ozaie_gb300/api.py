@@ -189,6 +189,16 @@ class Handle:
             out["q"] = q
         return out
 
+    def dump_pairs(self, A, B):
+        """The reference's device output (int64 lo, hi per element, shape [M, N, 2])."""
+        A = np.ascontiguousarray(A, np.float64)
+        B = np.ascontiguousarray(B, np.float64)
+        M, K = A.shape
+        N = B.shape[1]
+        out = np.zeros((M, N, 2), np.int64)
+        self._check(self._L.ozgb_dump_pairs(self._h, M, N, K, _ptr(A), _ptr(B), _ptr(out)))
+        return out
+
     def selftest_timeout(self, ms):
         return self._L.ozgb_selftest_timeout(self._h, float(ms))
 

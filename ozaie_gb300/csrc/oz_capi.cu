@@ -274,6 +274,7 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
     g.tiles_m = p.tiles_m;
     g.tiles_n = p.tiles_n;
     g.total_tiles = p.tiles_m * p.tiles_n;
+    if (out_mode == OUT_PAIRS) g.pair_g0 = reference_first_group(o.K, p.cfg.b, p.cfg.s);
 #ifdef OZGB_PROBE
     // probe builds: per-CTA cycle counters of the GEMM roles, summarised on stderr
     static unsigned long long *probe = nullptr;
@@ -323,7 +324,16 @@ ozgb_status enqueue_dgemm(ozgb_handle h, const Operands &o, int mode, cudaStream
     if ((rc = choose_config(h, o, mode, st, &cfg))) return rc;
     Plan p;
     std::string why;
-    if (!make_plan(o.M, o.N, o.K, cfg, &p, &why, bin_lo, bin_hi)) return fail(h, OZGB_ERR_UNSUPPORTED, why);
+    PlanHints pairs_hint;
+    const bool pairs = out_mode_override == OUT_PAIRS;
+    if (pairs) {
+        // the reference's paired output needs its d bins (triangular) and two
+        // 64-bit sums, i.e. a variant with at least 4 accumulator words
+        if (cfg.J != cfg.s) return fail(h, OZGB_ERR_UNSUPPORTED, "paired output needs the triangular pair set");
+        pairs_hint.min_W = 4;
+    }
+    if (!make_plan(o.M, o.N, o.K, cfg, &p, &why, bin_lo, bin_hi, pairs ? &pairs_hint : nullptr))
+        return fail(h, OZGB_ERR_UNSUPPORTED, why);
     h->last = p;
     h->have_last = true;
     const int om = out_mode_override >= 0 ? out_mode_override : cfg.rounding;
@@ -923,6 +933,28 @@ ozgb_status ozgb_get_config(ozgb_handle h, ozgb_config *out) {
 }
 
 const char *ozgb_last_error(ozgb_handle h) { return h ? h->msg.c_str() : "null handle"; }
+
+ozgb_status ozgb_dump_pairs(ozgb_handle h, int M, int N, int K, const double *A, const double *B, int64_t *pairs) {
+    if (!h || !A || !B || !pairs) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (M < 1 || N < 1 || K < 1) return fail(h, OZGB_ERR_DIMS, "dimensions must be positive");
+    ozgb_status rc = ensure_device(h);
+    if (rc) return rc;
+    cudaStream_t st = h->stream;
+    const size_t nA = static_cast<size_t>(M) * K, nB = static_cast<size_t>(K) * N, nC = static_cast<size_t>(M) * N;
+    if (!h->a.ensure(nA * 8) || !h->b.ensure(nB * 8) || !h->c.ensure(nC * 8) || !h->raw.ensure(nC * 16))
+        return fail(h, OZGB_ERR_ALLOC, "dump buffers");
+    cudaMemcpyAsync(h->a.p, A, nA * 8, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(h->b.p, B, nB * 8, cudaMemcpyHostToDevice, st);
+    Operands o{M, N, K, static_cast<double *>(h->a.p), K, static_cast<double *>(h->b.p), N,
+               static_cast<double *>(h->c.p), N};
+    if ((rc = enqueue_dgemm(h, o, h->setup_done ? h->mode : OZGB_MODE_FAST, st, OUT_PAIRS, 0, kMaxBins,
+                            static_cast<int32_t *>(h->raw.p))))
+        return rc;
+    if ((rc = check_device_error(h, st))) return rc;
+    const cudaError_t e = cudaMemcpy(pairs, h->raw.p, nC * 16, cudaMemcpyDeviceToHost);
+    return e == cudaSuccess ? OZGB_OK : cuda_fail(h, e, "pairs readback");
+}
 
 ozgb_status ozgb_dump(ozgb_handle h, int M, int N, int K, const double *A, const double *B, int32_t *er, int32_t *ec,
                       int8_t *a_slices, int8_t *b_slices, int32_t *q, int bin_lo, int bin_hi) {

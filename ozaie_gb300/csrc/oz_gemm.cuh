@@ -167,6 +167,29 @@ __device__ __forceinline__ void q_add_shifted(uint32_t (*q)[W], const uint32_t *
     }
 }
 
+// The reference's two 64-bit sums (OUT_PAIRS): bin j goes to the low word pair
+// q[0..1] with weight 2^(b t), t = J-1-j, when t < g0, else to q[2..3] with
+// weight 2^(b (t-g0)); both wrap modulo 2^64 like the reference's accumulators.
+template <int W, int NV>
+__device__ __forceinline__ void pairs_add(uint32_t (*q)[W], const uint32_t *v, int t, int b, int g0) {
+    if constexpr (W >= 4) {
+        const int base = t < g0 ? 0 : 2;
+        const int sh = b * (t < g0 ? t : t - g0);
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            const int32_t iv = __float2int_rz(__uint_as_float(v[i]));
+            const uint32_t ext = static_cast<uint32_t>(iv >> 31);
+            if (sh < 32) {
+                const uint32_t lo = static_cast<uint32_t>(iv) << sh;
+                const uint32_t hi = __funnelshift_l(static_cast<uint32_t>(iv), ext, sh);
+                asm("add.cc.u32 %0, %0, %2;\n\taddc.u32 %1, %1, %3;" : "+r"(q[i][base]), "+r"(q[i][base + 1]) : "r"(lo), "r"(hi));
+            } else {
+                q[i][base + 1] += static_cast<uint32_t>(iv) << (sh - 32);
+            }
+        }
+    }
+}
+
 // ------------------------------------------------------------ q -> double
 template <int W>
 __device__ __forceinline__ uint32_t qword(const uint32_t (&m)[W], int i) {
@@ -620,7 +643,10 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                                 tmem_ld_wait();
 #pragma unroll
                                 for (int i = 0; i < DB; ++i) reg_fence(v[i]);
-                                q_add_shifted<W, DB>(q + cb * DB, v, sh);
+                                if (g.out_mode == OUT_PAIRS)
+                                    pairs_add<W, DB>(q + cb * DB, v, g.J - 1 - j, g.b, g.pair_g0);
+                                else
+                                    q_add_shifted<W, DB>(q + cb * DB, v, sh);
                             }
                         }
                         // the block's accumulators are free for the next chunk (or tile)
@@ -641,7 +667,26 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
             if (row < tr.M) {
                 const int er = tr.er[row];
                 const int bJ1 = g.b * (g.J + 1);
-                if (g.out_mode == OUT_RAW) {
+                if (g.out_mode == OUT_PAIRS) {
+                    // the reference's device output: lo, then hi with bits 51..62 = Er + Ec
+                    if constexpr (W >= 4) {
+#pragma unroll
+                        for (int i = 0; i < COLS; ++i) {
+                            const int col = col0 + i;
+                            if (col < tr.N) {
+                                long long *dst =
+                                    reinterpret_cast<long long *>(g.raw) + (static_cast<size_t>(row) * tr.N + col) * 2;
+                                const unsigned long long lo = (static_cast<unsigned long long>(q[i][1]) << 32) | q[i][0];
+                                unsigned long long hi = (static_cast<unsigned long long>(q[i][3]) << 32) | q[i][2];
+                                const unsigned long long scale =
+                                    static_cast<unsigned long long>(static_cast<uint32_t>(er + tr.ec[col]));
+                                hi = (hi & 0x8007FFFFFFFFFFFFull) | ((scale & 0xFFFull) << 51);
+                                dst[0] = static_cast<long long>(lo);
+                                dst[1] = static_cast<long long>(hi);
+                            }
+                        }
+                    }
+                } else if (g.out_mode == OUT_RAW) {
 #pragma unroll
                     for (int i = 0; i < COLS; ++i) {
                         const int col = col0 + i;

@@ -27,7 +27,9 @@ constexpr int kEpiWarps = 16;     // drain + epilogue warps: 4 per TMEM lane qua
 constexpr int kThreads = 64 + 32 * kEpiWarps;  // warp 0 producer, warp 1 MMA issuer, then the drain warps
 constexpr int kMaxAccWords = 5;
 
-enum OutMode : int { OUT_RN = 0, OUT_RZ_REF = 1, OUT_RAW = 2 };
+// OUT_PAIRS writes the reference's device output (its C buffer before the host
+// decode): per element int64 lo, hi with (Er + Ec) in bits 51..62 of hi.
+enum OutMode : int { OUT_RN = 0, OUT_RZ_REF = 1, OUT_RAW = 2, OUT_PAIRS = 3 };
 
 // Shared memory after the pipeline stages: mbarriers, TMEM slot, abort flag
 // (plus 1 KB of alignment slack).
@@ -45,7 +47,7 @@ struct GemmArgs {
     const int32_t *ec;
     double *c;
     long ldc;
-    int32_t *raw;  // OUT_RAW: [M][N][4] words
+    int32_t *raw;  // OUT_RAW: [M][N][4] words; OUT_PAIRS: [M][N][2] int64
     int M, N;
     int n_kc, KC, s, J, b;
     int out_mode;
@@ -70,6 +72,7 @@ struct GemmArgs {
     int blk_lo[kMaxGroups], blk_nb[kMaxGroups], blk_p0[kMaxGroups], blk_p1[kMaxGroups];
     int blk_period[kMaxGroups], blk_off[kMaxGroups];
     int total_tiles;  // tiles_m * tiles_n
+    int pair_g0;      // OUT_PAIRS: bins in the low word group (the reference's first group)
 };
 
 // Work items of the grouped stage-(a)/(b) launch (k_stage_jobs): each job is one

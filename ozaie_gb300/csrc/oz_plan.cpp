@@ -28,6 +28,15 @@ constexpr size_t kSmemReserve = kCtrlBytes;
 
 }  // namespace
 
+int reference_first_group(int K, int b, int d) {
+    int ctz = 0;
+    while (ctz < 31 && !((K >> ctz) & 1)) ++ctz;
+    const int alignable = 31 / b + 1;
+    const int numer = b * (d + 1) - 51 + ctz;
+    const int minfirst = numer < 0 ? 1 : numer / b + 1;
+    return std::min(d, std::max(minfirst, alignable));
+}
+
 void reference_table(int K, int mode, int *b, int *d) {
     // include/oz_aie.h:60-80; the reference only reaches log2 K in [7, 11], the
     // table lists up to 14 and is clamped at both ends here.
@@ -138,6 +147,7 @@ bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string 
     for (const Variant &v : kVariants) {
         if (v.KC != 32) continue;
         if (hint.BN && v.BN != hint.BN) continue;
+        if (v.W < hint.min_W) continue;
         if (v.BN * J > 512) continue;
         if (32 * v.W < bits) continue;
         chosen = &v;

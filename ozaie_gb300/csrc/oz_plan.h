@@ -47,6 +47,7 @@ inline int pairs_in_bin(int j, int s) {
 struct PlanHints {
     int BN = 0, KC = 0, groups = 0, stages = 0;
     int sizes[kMaxGroups] = {0};  // explicit bin-block sizes (groups of them), overriding the cost model
+    int min_W = 0;                // at least this many accumulator words (4 for OUT_PAIRS)
 };
 
 // Builds the plan for bins [bin_lo, bin_hi] of the pair set (the full set of
@@ -66,6 +67,10 @@ void tune_store(int M, int N, int K, const OzConfig &cfg, const PlanHints &h);
 bool tune_lookup(int M, int N, int K, const OzConfig &cfg, PlanHints *h);
 void tune_clear();
 int tune_count();
+
+// Bins in the reference's first (low-word) sum group, ozaki_base.cc:151-158 with
+// log2 K = countr_zero(K) (include/oz_aie.h:100).
+int reference_first_group(int K, int b, int d);
 
 // The reference's (b, d) tables, include/oz_aie.h:60-80, indexed by log2 K.
 void reference_table(int K, int mode, int *b, int *d);

@@ -206,3 +206,23 @@ def test_device_timeout_path_is_recoverable(gpu_handle, oracle):
     gpu_handle.set_bins(8)
     C = _run(gpu_handle, A, B)
     assert np.array_equal(C.view(np.uint64), oracle.dgemm(A, B, 7, 8, 8, 0).view(np.uint64))
+
+
+@pytest.mark.parametrize("mode,shape", [(0, (256, 512, 128)), (1, (256, 512, 128)), (0, (130, 70, 1024)),
+                                        (1, (77, 91, 2048))])
+def test_reference_device_output_pairs(gpu_handle, oracle, mode, shape):
+    """The reference profile's paired int64 output equals the oracle's restatement
+    of the reference's device sum bit for bit, and decodes (with the reference's
+    host decode, pinned) to the profile's final results."""
+    M, N, K = shape
+    A = oracle.gen_phi((M, K), 71, 1.0)
+    B = oracle.gen_phi((K, N), 72, 1.0)
+    gpu_handle.set_profile(1)
+    C = _run(gpu_handle, A, B, mode)
+    cfg = gpu_handle.config()
+    b, d = cfg["bits"], cfg["slices"]
+    pairs = gpu_handle.dump_pairs(A, B)
+    er, ec, bins = _oracle_q(oracle, A, B, b, d, d)
+    want = oracle.sum_upshift(bins, er, ec, K, b, d)
+    assert np.array_equal(pairs, want)
+    assert np.array_equal(oracle.decode_pairs(pairs, K, d, b).view(np.uint64), C.view(np.uint64))
