@@ -97,6 +97,16 @@ ozgb_status ozgb_dgemm(ozgb_handle h, int M, int N, int K, const double *A, cons
  * (or OZGB_MODE_FAST when there was none). */
 ozgb_status ozgb_dgemm_device(ozgb_handle h, int M, int N, int K, const double *dA, long lda,
                               const double *dB, long ldb, double *dC, long ldc, void *stream);
+/* BLAS-style form on device arrays, row-major like the rest of the API:
+ *   C = alpha * op(A) op(B) + beta * C,  op(A) M x K, op(B) K x N,
+ * op(A) = A (stored M x K, lda >= K) or, with transa, A^T (A stored K x M,
+ * lda >= M); op(B) likewise (transb: B stored N x K, ldb >= K).  The product is
+ * the exact Ozaki result rounded once; alpha and beta are then applied in FP64
+ * (C is not read when beta == 0; A and B are not read when alpha == 0).  No
+ * reference counterpart: the reference computes C = A B on host arrays only
+ * (include/oz_aie.h:311). */
+ozgb_status ozgb_dgemm_ex(ozgb_handle h, int transa, int transb, int M, int N, int K, double alpha, const double *dA,
+                          long lda, const double *dB, long ldb, double beta, double *dC, long ldc, void *stream);
 /* Waits for the last enqueued call and checks the device error word. */
 ozgb_status ozgb_sync(ozgb_handle h);
 

@@ -88,6 +88,8 @@ SIGNATURES = [
     ("ozgb_plan_query", _i, [_i, _i, _i, _i, _i, _i, ctypes.POINTER(OzgbConfig)]),
     ("ozgb_choose_slices", _i, [_p, _p, _i, _p, _p, _i, _p, _p, _i, _i, _dbl, ctypes.POINTER(_dbl)]),
     ("ozgb_dgemm_device_noalloc", _i, [_i, _i, _i, _p, ctypes.c_long, _p, ctypes.c_long, _p, ctypes.c_long, _i, _p]),
+    ("ozgb_dgemm_ex", _i, [_h, _i, _i, _i, _i, _i, _dbl, _p, ctypes.c_long, _p, ctypes.c_long, _dbl, _p,
+                           ctypes.c_long, _p]),
     ("ozgb_dump_pairs", _i, [_h, _i, _i, _i, _p, _p, _p]),
     ("ozgb_autotune", _i, [_h, _i, _i, _i, _i, _i, _i, _i, ctypes.POINTER(OzgbConfig)]),
     ("ozgb_tuning_entries", _i, []),

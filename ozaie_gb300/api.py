@@ -102,6 +102,11 @@ class Handle:
         return self._L.ozgb_dgemm_device(self._h, M, N, K, ctypes.c_void_p(dA), lda, ctypes.c_void_p(dB), ldb,
                                          ctypes.c_void_p(dC), ldc, ctypes.c_void_p(stream or 0))
 
+    def dgemm_ex(self, transa, transb, M, N, K, alpha, dA, lda, dB, ldb, beta, dC, ldc, stream=None):
+        """C = alpha op(A) op(B) + beta C on device pointers (row-major, BLAS-style)."""
+        return self._L.ozgb_dgemm_ex(self._h, int(transa), int(transb), M, N, K, float(alpha), dA, lda, dB, ldb,
+                                     float(beta), dC, ldc, ctypes.c_void_p(stream or 0))
+
     def dgemm_grouped(self, problems, stream=None):
         arr = (OzgbProblem * len(problems))()
         for i, p in enumerate(problems):

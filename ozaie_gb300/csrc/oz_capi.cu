@@ -166,6 +166,8 @@ struct Operands {
     long ldb;
     double *C;
     long ldc;
+    bool ta = false, tb = false;  // A stored K x M, B stored N x K
+    double alpha = 1.0, beta = 0.0;
 };
 
 // Stage (a): exponents (+ sums of squares when the precision knob needs them).
@@ -181,8 +183,16 @@ ozgb_status enqueue_exponents(ozgb_handle h, const Operands &o, bool want_ss, cu
         cudaMemsetAsync(ssc, 0, sizeof(double) * o.N, st);
     }
     cudaMemsetAsync(h->ec.p, 0, sizeof(int32_t) * o.N, st);
-    launch_rowmax(o.A, o.lda, o.M, o.K, static_cast<int32_t *>(h->er.p), ssr, st);
-    launch_colmax(o.B, o.ldb, o.K, o.N, static_cast<int32_t *>(h->ec.p), ssc, st);
+    int32_t *er = static_cast<int32_t *>(h->er.p), *ec = static_cast<int32_t *>(h->ec.p);
+    if (o.ta) {
+        cudaMemsetAsync(er, 0, sizeof(int32_t) * o.M, st);
+        if (ssr) cudaMemsetAsync(ssr, 0, sizeof(double) * o.M, st);
+        launch_colmax(o.A, o.lda, o.K, o.M, er, ssr, st);  // rows of op(A) are columns of A
+    } else {
+        launch_rowmax(o.A, o.lda, o.M, o.K, er, ssr, st);
+    }
+    if (o.tb) launch_rowmax(o.B, o.ldb, o.N, o.K, ec, ssc, st);  // columns of op(B) are rows of B
+    else launch_colmax(o.B, o.ldb, o.K, o.N, ec, ssc, st);
     h->launches += 2;
     return OZGB_OK;
 }
@@ -201,8 +211,11 @@ ozgb_status choose_config(ozgb_handle h, const Operands &o, int mode, cudaStream
         int32_t *tmp = static_cast<int32_t *>(h->ktmp.p);
         cudaMemsetAsync(ca, 0, sizeof(double) * o.K, st);
         cudaMemsetAsync(tmp, 0, sizeof(int32_t) * o.K, st);
-        launch_colmax(o.A, o.lda, o.M, o.K, tmp, ca, st);
-        launch_rowmax(o.B, o.ldb, o.K, o.N, tmp, rb, st);
+        // ca[k] = |op(A)(:,k)|^2, rb[k] = |op(B)(k,:)|^2
+        if (o.ta) launch_rowmax(o.A, o.lda, o.K, o.M, tmp, ca, st);
+        else launch_colmax(o.A, o.lda, o.M, o.K, tmp, ca, st);
+        if (o.tb) launch_colmax(o.B, o.ldb, o.N, o.K, tmp, rb, st);
+        else launch_rowmax(o.B, o.ldb, o.K, o.N, tmp, rb, st);
         launch_knob_stats(static_cast<int32_t *>(h->er.p), static_cast<double *>(h->ssr.p), o.M,
                           static_cast<int32_t *>(h->ec.p), static_cast<double *>(h->ssc.p), o.N, ca, rb, o.K,
                           static_cast<double *>(h->knob.p), st);
@@ -237,6 +250,8 @@ void gemm_args_from_plan(GemmArgs *g, const Plan &p, int out_mode, int *err, uns
     g->tmem_cols = p.tmem_cols;
     g->err = err;
     g->timeout_ns = timeout_ns;
+    g->alpha = 1.0;
+    g->beta = 0.0;
     g->G = p.G;
     for (int i = 0; i < p.G; ++i) {
         g->blk_lo[i] = p.blk_lo[i];
@@ -254,9 +269,10 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
     if (!h->at.ensure(p.a_elems * 2) || !h->bt.ensure(p.b_elems * 2))
         return fail(h, OZGB_ERR_ALLOC, "slice buffers");
     uint16_t *at = static_cast<uint16_t *>(h->at.p), *bt = static_cast<uint16_t *>(h->bt.p);
-    launch_split_a(o.A, o.lda, o.M, o.K, static_cast<int32_t *>(h->er.p), p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.Mp, at, st);
+    launch_split_a(o.A, o.lda, o.M, o.K, static_cast<int32_t *>(h->er.p), p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.Mp, at, st,
+                   o.ta);
     launch_split_b(o.B, o.ldb, o.K, o.N, static_cast<int32_t *>(h->ec.p), p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.BN, p.Np,
-                   bt, st);
+                   bt, st, o.tb);
     h->launches += 2;
     if (h->profiling) cudaEventRecord(h->ev[2], st);
     GemmArgs g;
@@ -274,6 +290,8 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
     g.tiles_m = p.tiles_m;
     g.tiles_n = p.tiles_n;
     g.total_tiles = p.tiles_m * p.tiles_n;
+    g.alpha = o.alpha;
+    g.beta = o.beta;
     if (out_mode == OUT_PAIRS) g.pair_g0 = reference_first_group(o.K, p.cfg.b, p.cfg.s);
 #ifdef OZGB_PROBE
     // probe builds: per-CTA cycle counters of the GEMM roles, summarised on stderr
@@ -804,6 +822,34 @@ ozgb_status ozgb_dgemm_device(ozgb_handle h, int M, int N, int K, const double *
     if (rc) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL: the default (legacy) stream
     Operands o{M, N, K, dA, lda, dB, ldb, dC, ldc};
+    return enqueue_dgemm(h, o, h->setup_done ? h->mode : OZGB_MODE_FAST, st);
+}
+
+ozgb_status ozgb_dgemm_ex(ozgb_handle h, int transa, int transb, int M, int N, int K, double alpha, const double *dA,
+                          long lda, const double *dB, long ldb, double beta, double *dC, long ldc, void *stream) {
+    if (!h) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (M < 1 || N < 1 || K < 1) return fail(h, OZGB_ERR_DIMS, "dimensions must be positive");
+    if (!dA || !dB || !dC) return fail(h, OZGB_ERR_ARG, "null matrix pointer");
+    if ((transa ? lda < M : lda < K) || (transb ? ldb < K : ldb < N) || ldc < N)
+        return fail(h, OZGB_ERR_ARG, "leading dimension too small");
+    if (!std::isfinite(alpha) || !std::isfinite(beta)) return fail(h, OZGB_ERR_ARG, "alpha and beta must be finite");
+    ozgb_status rc = ensure_device(h);
+    if (rc) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    Operands o{M, N, K, dA, lda, dB, ldb, dC, ldc};
+    o.ta = transa != 0;
+    o.tb = transb != 0;
+    o.alpha = alpha;
+    o.beta = beta;
+    if (alpha == 0.0) {
+        // C = beta * C: A and B are not read, as BLAS does
+        h->last_stream = st;
+        launch_scale(dC, ldc, M, N, beta, st);
+        h->launches += 1;
+        const cudaError_t e = cudaGetLastError();
+        return e == cudaSuccess ? OZGB_OK : cuda_fail(h, e, "scale launch");
+    }
     return enqueue_dgemm(h, o, h->setup_done ? h->mode : OZGB_MODE_FAST, st);
 }
 

@@ -699,10 +699,16 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                     }
                 } else {
                     double *crow = tr.c + static_cast<size_t>(row) * tr.ldc;
+                    const bool plain = g.alpha == 1.0 && g.beta == 0.0;
 #pragma unroll
                     for (int i = 0; i < COLS; ++i) {
                         const int col = col0 + i;
-                        if (col < tr.N) crow[col] = q_to_double<W>(q[i], er + tr.ec[col], bJ1, g.out_mode);
+                        if (col < tr.N) {
+                            double v = q_to_double<W>(q[i], er + tr.ec[col], bJ1, g.out_mode);
+                            // BLAS semantics: C is not read when beta == 0
+                            if (!plain) v = g.beta == 0.0 ? g.alpha * v : fma(g.beta, crow[col], g.alpha * v);
+                            crow[col] = v;
+                        }
                     }
                 }
             }

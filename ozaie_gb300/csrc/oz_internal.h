@@ -73,6 +73,7 @@ struct GemmArgs {
     int blk_period[kMaxGroups], blk_off[kMaxGroups];
     int total_tiles;  // tiles_m * tiles_n
     int pair_g0;      // OUT_PAIRS: bins in the low word group (the reference's first group)
+    double alpha, beta;  // C = alpha * (A B) + beta * C for OUT_RN / OUT_RZ_REF (1, 0: plain store)
 };
 
 // Work items of the grouped stage-(a)/(b) launch (k_stage_jobs): each job is one
@@ -124,10 +125,11 @@ OZ_GEMM_VARIANTS(OZ_DECLARE_GEMM)
 // Stage (a) / (b) launches (oz_split.cu).
 void launch_rowmax(const double *A, long lda, int M, int K, int32_t *er, double *ss, void *stream);
 void launch_colmax(const double *B, long ldb, int K, int N, int32_t *ec, double *ss, void *stream);
+// trans: A is stored K x M (element (m, k) at A[k * lda + m]); B is stored N x K.
 void launch_split_a(const double *A, long lda, int M, int K, const int32_t *er, int b, int s, int KC, int n_kc,
-                    int Mp, uint16_t *tiles, void *stream);
+                    int Mp, uint16_t *tiles, void *stream, bool trans = false);
 void launch_split_b(const double *B, long ldb, int K, int N, const int32_t *ec, int b, int s, int KC, int n_kc,
-                    int BN, int Np, uint16_t *tiles, void *stream);
+                    int BN, int Np, uint16_t *tiles, void *stream, bool trans = false);
 int launch_selftest_timeout(int *err, unsigned long long timeout_ns, void *stream);
 // Precision-knob statistics (five doubles, see KnobStats in oz_plan.h) from the
 // row/column exponents and sums of squares of stage (a) and the per-k sums of
@@ -140,6 +142,8 @@ void stage_grid(const StageJob &j, int *gx, int *gy);
 // block0[n_jobs] = total), and the knob reduction of n problems.
 void launch_stage_jobs(const StageJob *jobs, const int *block0, int n_jobs, int total_blocks, void *stream);
 void launch_knob_grouped(const KnobJob *jobs, int n, void *stream);
+// C = beta * C (zeros for beta == 0, C not read).
+void launch_scale(double *C, long ldc, int M, int N, double beta, void *stream);
 // Pseudo-random doubles in [-1, 1) for timing runs.
 void launch_fill_random(double *x, size_t n, unsigned long long seed, void *stream);
 

@@ -135,6 +135,8 @@ extern "C" ozgb_status ozgb_dgemm_device_noalloc(int M, int N, int K, const doub
     g.tiles_m = p.tiles_m;
     g.tiles_n = p.tiles_n;
     g.total_tiles = p.tiles_m * p.tiles_n;
+    g.alpha = 1.0;  // C = A B
+    g.beta = 0.0;
     g.stages = p.stages;
     g.stage_bytes = p.stage_bytes;
     g.a_block_bytes = p.a_block_bytes;

@@ -125,7 +125,8 @@ __host__ __device__ inline bool split_two_windows(int b, int s) {
 // consecutive K values of one row and writes one 16-byte piece per slice; a warp
 // covers 8 rows x 32 K (4 core matrices of each slice, 512 contiguous bytes).
 __device__ __forceinline__ void split_a_body(const double *__restrict__ A, long lda, int M, int K, const int32_t *__restrict__ er,
-                          int b, int s, int KC, int n_kc, int Mp, uint16_t *__restrict__ tiles, int bx, int by) {
+                          int b, int s, int KC, int n_kc, int Mp, uint16_t *__restrict__ tiles, int bx, int by,
+                          bool trans = false) {
     const int r8 = threadIdx.x & 7;
     const int kgl = threadIdx.x >> 3;  // 0..31
     const int m = by * 8 + r8;
@@ -139,7 +140,7 @@ __device__ __forceinline__ void split_a_body(const double *__restrict__ A, long 
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         const int k = k0 + i;
-        const double x = (m < M && k < K) ? __ldg(row + k) : 0.0;
+        const double x = (m < M && k < K) ? __ldg(trans ? A + static_cast<size_t>(k) * lda + m : row + k) : 0.0;
         st[i] = split_value(x, E, two);
     }
     const int mt = m >> 7, r = m & 127, c = k0 / KC, kk = k0 % KC;
@@ -155,15 +156,16 @@ __device__ __forceinline__ void split_a_body(const double *__restrict__ A, long 
     }
 }
 __global__ void k_split_a(const double *__restrict__ A, long lda, int M, int K, const int32_t *__restrict__ er,
-                          int b, int s, int KC, int n_kc, int Mp, uint16_t *__restrict__ tiles) {
-    split_a_body(A, lda, M, K, er, b, s, KC, n_kc, Mp, tiles, blockIdx.x, blockIdx.y);
+                          int b, int s, int KC, int n_kc, int Mp, uint16_t *__restrict__ tiles, int trans) {
+    split_a_body(A, lda, M, K, er, b, s, KC, n_kc, Mp, tiles, blockIdx.x, blockIdx.y, trans != 0);
 }
 
 // B [K][N] row-major -> slice blocks of B^T [nt][c][q][BN x KC].  One thread
 // takes one column n and 8 consecutive K; a warp reads 32 consecutive columns
 // per row (coalesced) and writes four 128-byte core matrices per slice.
 __device__ __forceinline__ void split_b_body(const double *__restrict__ B, long ldb, int K, int N, const int32_t *__restrict__ ec,
-                          int b, int s, int KC, int n_kc, int BN, int Np, uint16_t *__restrict__ tiles, int bx, int by) {
+                          int b, int s, int KC, int n_kc, int BN, int Np, uint16_t *__restrict__ tiles, int bx, int by,
+                          bool trans = false) {
     const int n = bx * 32 + (threadIdx.x & 31);
     const int k0 = (by * 8 + (threadIdx.x >> 5)) * 8;
     const int Kp = n_kc * KC;
@@ -174,7 +176,9 @@ __device__ __forceinline__ void split_b_body(const double *__restrict__ B, long 
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         const int k = k0 + i;
-        const double x = (n < N && k < K) ? __ldg(B + static_cast<size_t>(k) * ldb + n) : 0.0;
+        const double x =
+            (n < N && k < K) ? __ldg(trans ? B + static_cast<size_t>(n) * ldb + k : B + static_cast<size_t>(k) * ldb + n)
+                             : 0.0;
         st[i] = split_value(x, E, two);
     }
     const int nt = n / BN, r = n % BN, c = k0 / KC, kk = k0 % KC;
@@ -190,8 +194,8 @@ __device__ __forceinline__ void split_b_body(const double *__restrict__ B, long 
     }
 }
 __global__ void k_split_b(const double *__restrict__ B, long ldb, int K, int N, const int32_t *__restrict__ ec,
-                          int b, int s, int KC, int n_kc, int BN, int Np, uint16_t *__restrict__ tiles) {
-    split_b_body(B, ldb, K, N, ec, b, s, KC, n_kc, BN, Np, tiles, blockIdx.x, blockIdx.y);
+                          int b, int s, int KC, int n_kc, int BN, int Np, uint16_t *__restrict__ tiles, int trans) {
+    split_b_body(B, ldb, K, N, ec, b, s, KC, n_kc, BN, Np, tiles, blockIdx.x, blockIdx.y, trans != 0);
 }
 
 // A kernel whose only wait is on an mbarrier that nothing arrives on: exercises
@@ -337,6 +341,21 @@ void launch_fill_random(double *x, size_t n, unsigned long long seed, void *stre
     if (n) k_fill_random<<<4 * 152, 256, 0, static_cast<cudaStream_t>(stream)>>>(x, n, seed);
 }
 
+// C = beta * C over an M x N block with leading dimension ldc (beta == 0 writes
+// zeros without reading C, as BLAS does).
+__global__ void k_scale(double *__restrict__ C, long ldc, int M, int N, double beta) {
+    const size_t total = static_cast<size_t>(M) * N;
+    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        double *c = C + (i / N) * ldc + (i % N);
+        *c = beta == 0.0 ? 0.0 : beta * *c;
+    }
+}
+
+void launch_scale(double *C, long ldc, int M, int N, double beta, void *stream) {
+    k_scale<<<4 * 152, 256, 0, static_cast<cudaStream_t>(stream)>>>(C, ldc, M, N, beta);
+}
+
 void stage_grid(const StageJob &j, int *gx, int *gy) {
     switch (j.kind) {
         case JOB_ROWMAX:
@@ -386,18 +405,19 @@ void launch_colmax(const double *B, long ldb, int K, int N, int32_t *ec, double 
 }
 
 void launch_split_a(const double *A, long lda, int M, int K, const int32_t *er, int b, int s, int KC, int n_kc,
-                    int Mp, uint16_t *tiles, void *stream) {
+                    int Mp, uint16_t *tiles, void *stream, bool trans) {
     const int Kp = n_kc * KC;
     dim3 grid((Kp / 8 + 31) / 32, Mp / 8);
-    k_split_a<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(A, lda, M, K, er, b, s, KC, n_kc, Mp, tiles);
+    k_split_a<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(A, lda, M, K, er, b, s, KC, n_kc, Mp, tiles,
+                                                                    trans ? 1 : 0);
 }
 
 void launch_split_b(const double *B, long ldb, int K, int N, const int32_t *ec, int b, int s, int KC, int n_kc,
-                    int BN, int Np, uint16_t *tiles, void *stream) {
+                    int BN, int Np, uint16_t *tiles, void *stream, bool trans) {
     const int Kp = n_kc * KC;
     dim3 grid((Np + 31) / 32, (Kp / 8 + 7) / 8);
     k_split_b<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(B, ldb, K, N, ec, b, s, KC, n_kc, BN, Np,
-                                                                    tiles);
+                                                                    tiles, trans ? 1 : 0);
 }
 
 int launch_selftest_timeout(int *err, unsigned long long timeout_ns, void *stream) {
