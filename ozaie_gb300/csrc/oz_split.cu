@@ -8,6 +8,7 @@
 // the optional sum of squares that the precision knob reads.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "oz_internal.h"
@@ -107,12 +108,27 @@ __device__ __forceinline__ SplitState split_value(double x, int E, bool two_wind
     return st;
 }
 
-__device__ __forceinline__ uint32_t slice_bf16(const SplitState &st, int i, int b) {
-    const int sh = 128 - b * (i + 1);
-    int v = sh >= 0 ? static_cast<int>(static_cast<uint32_t>(st.X >> sh) & ((1u << b) - 1u)) : 0;
-    if (st.neg) v = -v;
-    // |v| <= 127 is exact in bf16: the top half of the fp32 pattern
-    return __float_as_uint(static_cast<float>(v)) >> 16;
+// The split window as four 32-bit words, most significant first (w[4] = 0 so that
+// a slice straddling two words is one funnel shift), and the bf16 sign bit.
+__device__ __forceinline__ void split_words(const SplitState &st, uint32_t (&w)[5], uint32_t &sign) {
+    w[0] = static_cast<uint32_t>(st.X >> 96);
+    w[1] = static_cast<uint32_t>(st.X >> 64);
+    w[2] = static_cast<uint32_t>(st.X >> 32);
+    w[3] = static_cast<uint32_t>(st.X);
+    w[4] = 0u;
+    sign = st.neg ? 0x8000u : 0u;
+}
+
+// bf16 bits of slice p (b = B bits at bit position B*p from the top), signed:
+// the magnitude v < 2^8 becomes a float through the FP32 adder (2^23 + v - 2^23,
+// exact) rather than the slower integer conversion; +0 for zero slices.
+template <int B>
+__device__ __forceinline__ uint32_t slice_bits(const uint32_t (&w)[5], uint32_t sign, int p) {
+    const int pos = B * p;
+    const int idx = pos >> 5, off = pos & 31;
+    const uint32_t v = __funnelshift_l(w[idx + 1], w[idx], off) >> (32 - B);
+    const uint32_t mag = __float_as_uint(__uint_as_float(0x4B000000u | v) - 8388608.0f) >> 16;
+    return mag | (v ? sign : 0u);
 }
 
 __host__ __device__ inline bool split_two_windows(int b, int s) {
@@ -124,79 +140,101 @@ __host__ __device__ inline bool split_two_windows(int b, int s) {
 // A [M][K] row-major -> A slice blocks [mt][c][p][128 x KC].  One thread takes 8
 // consecutive K values of one row and writes one 16-byte piece per slice; a warp
 // covers 8 rows x 32 K (4 core matrices of each slice, 512 contiguous bytes).
-__device__ __forceinline__ void split_a_body(const double *__restrict__ A, long lda, int M, int K, const int32_t *__restrict__ er,
-                          int b, int s, int KC, int n_kc, int Mp, uint16_t *__restrict__ tiles, int bx, int by,
-                          bool trans = false) {
+template <int B>
+__device__ __forceinline__ void split_a_body(const double *__restrict__ A, long lda, int M, int K,
+                                             const int32_t *__restrict__ er, int s, int KC, int n_kc, int Mp,
+                                             uint16_t *__restrict__ tiles, int bx, int by, bool trans) {
     const int r8 = threadIdx.x & 7;
     const int kgl = threadIdx.x >> 3;  // 0..31
     const int m = by * 8 + r8;
     const int k0 = (bx * 32 + kgl) * 8;
     const int Kp = n_kc * KC;
     if (m >= Mp || k0 >= Kp) return;
-    const bool two = split_two_windows(b, s);
+    const bool two = split_two_windows(B, s);
     const int E = m < M ? er[m] : 0;
-    SplitState st[8];
+    uint32_t w[8][5], sg[8];
     const double *row = A + static_cast<size_t>(m) * lda;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         const int k = k0 + i;
         const double x = (m < M && k < K) ? __ldg(trans ? A + static_cast<size_t>(k) * lda + m : row + k) : 0.0;
-        st[i] = split_value(x, E, two);
+        split_words(split_value(x, E, two), w[i], sg[i]);
     }
     const int mt = m >> 7, r = m & 127, c = k0 / KC, kk = k0 % KC;
     const size_t slice_elems = static_cast<size_t>(BM) * KC;
     uint16_t *dst = tiles + (static_cast<size_t>(mt) * n_kc + c) * s * slice_elems + canon_offset(r, kk, KC);
-    for (int p = 0; p < s; ++p) {
-        uint4 v;
-        v.x = slice_bf16(st[0], p, b) | (slice_bf16(st[1], p, b) << 16);
-        v.y = slice_bf16(st[2], p, b) | (slice_bf16(st[3], p, b) << 16);
-        v.z = slice_bf16(st[4], p, b) | (slice_bf16(st[5], p, b) << 16);
-        v.w = slice_bf16(st[6], p, b) | (slice_bf16(st[7], p, b) << 16);
-        *reinterpret_cast<uint4 *>(dst + p * slice_elems) = v;
+#pragma unroll
+    for (int p = 0; p < 128 / B; ++p) {
+        if (p < s) {
+            uint4 v;
+            v.x = slice_bits<B>(w[0], sg[0], p) | (slice_bits<B>(w[1], sg[1], p) << 16);
+            v.y = slice_bits<B>(w[2], sg[2], p) | (slice_bits<B>(w[3], sg[3], p) << 16);
+            v.z = slice_bits<B>(w[4], sg[4], p) | (slice_bits<B>(w[5], sg[5], p) << 16);
+            v.w = slice_bits<B>(w[6], sg[6], p) | (slice_bits<B>(w[7], sg[7], p) << 16);
+            *reinterpret_cast<uint4 *>(dst + p * slice_elems) = v;
+        }
     }
 }
+template <int B>
 __global__ void k_split_a(const double *__restrict__ A, long lda, int M, int K, const int32_t *__restrict__ er,
-                          int b, int s, int KC, int n_kc, int Mp, uint16_t *__restrict__ tiles, int trans) {
-    split_a_body(A, lda, M, K, er, b, s, KC, n_kc, Mp, tiles, blockIdx.x, blockIdx.y, trans != 0);
+                          int s, int KC, int n_kc, int Mp, uint16_t *__restrict__ tiles, int trans) {
+    split_a_body<B>(A, lda, M, K, er, s, KC, n_kc, Mp, tiles, blockIdx.x, blockIdx.y, trans != 0);
 }
 
 // B [K][N] row-major -> slice blocks of B^T [nt][c][q][BN x KC].  One thread
 // takes one column n and 8 consecutive K; a warp reads 32 consecutive columns
 // per row (coalesced) and writes four 128-byte core matrices per slice.
-__device__ __forceinline__ void split_b_body(const double *__restrict__ B, long ldb, int K, int N, const int32_t *__restrict__ ec,
-                          int b, int s, int KC, int n_kc, int BN, int Np, uint16_t *__restrict__ tiles, int bx, int by,
-                          bool trans = false) {
+template <int B>
+__device__ __forceinline__ void split_b_body(const double *__restrict__ Bm, long ldb, int K, int N,
+                                             const int32_t *__restrict__ ec, int s, int KC, int n_kc, int BN, int Np,
+                                             uint16_t *__restrict__ tiles, int bx, int by, bool trans) {
     const int n = bx * 32 + (threadIdx.x & 31);
     const int k0 = (by * 8 + (threadIdx.x >> 5)) * 8;
     const int Kp = n_kc * KC;
     if (n >= Np || k0 >= Kp) return;
-    const bool two = split_two_windows(b, s);
+    const bool two = split_two_windows(B, s);
     const int E = n < N ? ec[n] : 0;
-    SplitState st[8];
+    uint32_t w[8][5], sg[8];
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         const int k = k0 + i;
         const double x =
-            (n < N && k < K) ? __ldg(trans ? B + static_cast<size_t>(n) * ldb + k : B + static_cast<size_t>(k) * ldb + n)
+            (n < N && k < K) ? __ldg(trans ? Bm + static_cast<size_t>(n) * ldb + k : Bm + static_cast<size_t>(k) * ldb + n)
                              : 0.0;
-        st[i] = split_value(x, E, two);
+        split_words(split_value(x, E, two), w[i], sg[i]);
     }
     const int nt = n / BN, r = n % BN, c = k0 / KC, kk = k0 % KC;
     const size_t slice_elems = static_cast<size_t>(BN) * KC;
     uint16_t *dst = tiles + (static_cast<size_t>(nt) * n_kc + c) * s * slice_elems + canon_offset(r, kk, KC);
-    for (int q = 0; q < s; ++q) {
-        uint4 v;
-        v.x = slice_bf16(st[0], q, b) | (slice_bf16(st[1], q, b) << 16);
-        v.y = slice_bf16(st[2], q, b) | (slice_bf16(st[3], q, b) << 16);
-        v.z = slice_bf16(st[4], q, b) | (slice_bf16(st[5], q, b) << 16);
-        v.w = slice_bf16(st[6], q, b) | (slice_bf16(st[7], q, b) << 16);
-        *reinterpret_cast<uint4 *>(dst + q * slice_elems) = v;
+#pragma unroll
+    for (int q = 0; q < 128 / B; ++q) {
+        if (q < s) {
+            uint4 v;
+            v.x = slice_bits<B>(w[0], sg[0], q) | (slice_bits<B>(w[1], sg[1], q) << 16);
+            v.y = slice_bits<B>(w[2], sg[2], q) | (slice_bits<B>(w[3], sg[3], q) << 16);
+            v.z = slice_bits<B>(w[4], sg[4], q) | (slice_bits<B>(w[5], sg[5], q) << 16);
+            v.w = slice_bits<B>(w[6], sg[6], q) | (slice_bits<B>(w[7], sg[7], q) << 16);
+            *reinterpret_cast<uint4 *>(dst + q * slice_elems) = v;
+        }
     }
 }
-__global__ void k_split_b(const double *__restrict__ B, long ldb, int K, int N, const int32_t *__restrict__ ec,
-                          int b, int s, int KC, int n_kc, int BN, int Np, uint16_t *__restrict__ tiles, int trans) {
-    split_b_body(B, ldb, K, N, ec, b, s, KC, n_kc, BN, Np, tiles, blockIdx.x, blockIdx.y, trans != 0);
+template <int B>
+__global__ void k_split_b(const double *__restrict__ Bm, long ldb, int K, int N, const int32_t *__restrict__ ec,
+                          int s, int KC, int n_kc, int BN, int Np, uint16_t *__restrict__ tiles, int trans) {
+    split_b_body<B>(Bm, ldb, K, N, ec, s, KC, n_kc, BN, Np, tiles, blockIdx.x, blockIdx.y, trans != 0);
 }
+
+// b (1..7) as a template argument: the slice positions become constants.
+#define OZ_SPLIT_DISPATCH(b, CALL) \
+    switch (b) {                   \
+        case 1: CALL(1); break;    \
+        case 2: CALL(2); break;    \
+        case 3: CALL(3); break;    \
+        case 4: CALL(4); break;    \
+        case 5: CALL(5); break;    \
+        case 6: CALL(6); break;    \
+        default: CALL(7); break;   \
+    }
 
 // A kernel whose only wait is on an mbarrier that nothing arrives on: exercises
 // the bounded-wait path (records DEVERR_TIMEOUT_SELFTEST and returns).
@@ -244,10 +282,25 @@ __device__ double block_sum(double v, double *sh) {
 //   out[2] = sum_j 4^{Ec_j-eb}           out[3] = sum_j |b_j|^2 4^{1022-eb}
 //   out[4] = sum_k |A(:,k)|^2 |B(k,:)|^2 4^{2044-ea-eb}
 // Block 0 makes the A terms, block 1 the B terms, block 2 the K-direction term.
+// 2^e as an exact double for e in [-1022, 1023] (0 below: those terms are
+// negligible in the knob's sums).
+__device__ __forceinline__ double pow2i(int e) {
+    if (e < -1022) return 0.0;
+    return __longlong_as_double(static_cast<long long>(min(e, 1023) + 1023) << 52);
+}
+// x * 2^e for e in [-2046, 2046], as two exact power-of-two products.
+__device__ __forceinline__ double scale2(double x, int e) {
+    const int h = e / 2;
+    return x * pow2i(h) * pow2i(e - h);
+}
+
+// Part `chunk` of `chunks` of one of the three sums (role 0: A terms, 1: B
+// terms, 2: the k-direction term), added atomically into out (zeroed before).
 __device__ __forceinline__ void knob_stats_body(const int32_t *__restrict__ er, const double *__restrict__ ssr, int M,
                                                 const int32_t *__restrict__ ec, const double *__restrict__ ssc, int N,
                                                 const double *__restrict__ ca, const double *__restrict__ rb, int K,
-                                                double *__restrict__ out, const int role) {
+                                                double *__restrict__ out, const int role, const int chunk,
+                                                const int chunks) {
     __shared__ int sh_i[32];
     __shared__ double sh_d[32];
     int ea = 0, eb = 0;
@@ -259,28 +312,30 @@ __device__ __forceinline__ void knob_stats_body(const int32_t *__restrict__ er, 
         for (int j = threadIdx.x; j < N; j += blockDim.x) eb = max(eb, ec[j]);
         eb = block_max_int(eb, sh_i);
     }
+    const int n = role == 0 ? M : (role == 1 ? N : K);
+    const int per = (n + chunks - 1) / chunks;
+    const int i0 = chunk * per, i1 = min(n, i0 + per);
     if (role < 2) {
         const int32_t *e = role == 0 ? er : ec;
         const double *ss = role == 0 ? ssr : ssc;
-        const int n = role == 0 ? M : N;
         const int emax = role == 0 ? ea : eb;
         double num = 0.0, den = 0.0;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            num += ldexp(1.0, 2 * (e[i] - emax));
-            den += ldexp(ss[i], -2 * (emax - 1022));
+        for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+            num += pow2i(2 * (e[i] - emax));
+            den += scale2(ss[i], -2 * (emax - 1022));
         }
         num = block_sum(num, sh_d);
         den = block_sum(den, sh_d);
         if (threadIdx.x == 0) {
-            out[2 * role] = num;
-            out[2 * role + 1] = den;
+            atomicAdd(out + 2 * role, num);
+            atomicAdd(out + 2 * role + 1, den);
         }
     } else {
         double t = 0.0;
-        for (int k = threadIdx.x; k < K; k += blockDim.x)
-            t += ldexp(ca[k], -2 * (ea - 1022)) * ldexp(rb[k], -2 * (eb - 1022));
+        for (int k = i0 + threadIdx.x; k < i1; k += blockDim.x)
+            t += scale2(ca[k], -2 * (ea - 1022)) * scale2(rb[k], -2 * (eb - 1022));
         t = block_sum(t, sh_d);
-        if (threadIdx.x == 0) out[4] = t;
+        if (threadIdx.x == 0) atomicAdd(out + 4, t);
     }
 }
 
@@ -289,13 +344,13 @@ __global__ void k_knob_stats(const int32_t *__restrict__ er, const double *__res
                              const int32_t *__restrict__ ec, const double *__restrict__ ssc, int N,
                              const double *__restrict__ ca, const double *__restrict__ rb, int K,
                              double *__restrict__ out) {
-    knob_stats_body(er, ssr, M, ec, ssc, N, ca, rb, K, out, blockIdx.x);
+    knob_stats_body(er, ssr, M, ec, ssc, N, ca, rb, K, out, blockIdx.x % 3, blockIdx.x / 3, gridDim.x / 3);
 }
 
 // Grouped knob reduction: blocks 3p, 3p+1, 3p+2 reduce problem p.
 __global__ void k_knob_grouped(const KnobJob *__restrict__ jobs) {
     const KnobJob j = jobs[blockIdx.x / 3];
-    knob_stats_body(j.er, j.ssr, j.M, j.ec, j.ssc, j.N, j.ca, j.rb, j.K, j.out, blockIdx.x % 3);
+    knob_stats_body(j.er, j.ssr, j.M, j.ec, j.ssc, j.N, j.ca, j.rb, j.K, j.out, blockIdx.x % 3, 0, 1);
 }
 
 // Grouped stage (a)/(b): block -> job by binary search over block0[], then the
@@ -315,12 +370,19 @@ __global__ void __launch_bounds__(kStageThreads) k_stage_jobs(const StageJob *__
     switch (j.kind) {
         case JOB_ROWMAX: rowmax_body(j.X, j.ld, j.rows, j.cols, j.e_out, j.ss_out, bx, by); break;
         case JOB_COLMAX: colmax_body(j.X, j.ld, j.rows, j.cols, 64, j.e_out, j.ss_out, bx, by); break;
-        case JOB_SPLIT_A:
-            split_a_body(j.X, j.ld, j.rows, j.cols, j.e_in, j.b, j.s, j.KC, j.n_kc, j.padded, j.tiles, bx, by);
+        case JOB_SPLIT_A: {
+#define OZ_JOB_A(BB) split_a_body<BB>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.padded, j.tiles, bx, by, false)
+            OZ_SPLIT_DISPATCH(j.b, OZ_JOB_A)
+#undef OZ_JOB_A
             break;
-        default:
-            split_b_body(j.X, j.ld, j.rows, j.cols, j.e_in, j.b, j.s, j.KC, j.n_kc, j.BN, j.padded, j.tiles, bx, by);
+        }
+        default: {
+#define OZ_JOB_B(BB) \
+    split_b_body<BB>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.BN, j.padded, j.tiles, bx, by, false)
+            OZ_SPLIT_DISPATCH(j.b, OZ_JOB_B)
+#undef OZ_JOB_B
             break;
+        }
     }
 }
 
@@ -388,7 +450,10 @@ void launch_knob_grouped(const KnobJob *jobs, int n, void *stream) {
 
 void launch_knob_stats(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N,
                        const double *ca, const double *rb, int K, double *out, void *stream) {
-    k_knob_stats<<<3, 1024, 0, static_cast<cudaStream_t>(stream)>>>(er, ssr, M, ec, ssc, N, ca, rb, K, out);
+    // each of the three sums split over up to 32 blocks of 256 threads
+    const int chunks = std::max(1, std::min(32, std::max(M, std::max(N, K)) / 1024));
+    cudaMemsetAsync(out, 0, 5 * sizeof(double), static_cast<cudaStream_t>(stream));
+    k_knob_stats<<<3 * chunks, 256, 0, static_cast<cudaStream_t>(stream)>>>(er, ssr, M, ec, ssc, N, ca, rb, K, out);
 }
 
 void launch_rowmax(const double *A, long lda, int M, int K, int32_t *er, double *ss, void *stream) {
@@ -408,16 +473,22 @@ void launch_split_a(const double *A, long lda, int M, int K, const int32_t *er, 
                     int Mp, uint16_t *tiles, void *stream, bool trans) {
     const int Kp = n_kc * KC;
     dim3 grid((Kp / 8 + 31) / 32, Mp / 8);
-    k_split_a<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(A, lda, M, K, er, b, s, KC, n_kc, Mp, tiles,
-                                                                    trans ? 1 : 0);
+#define OZ_CALL_A(BB)                                                                                  \
+    k_split_a<BB><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(A, lda, M, K, er, s, KC, n_kc, Mp, tiles, \
+                                                                        trans ? 1 : 0)
+    OZ_SPLIT_DISPATCH(b, OZ_CALL_A)
+#undef OZ_CALL_A
 }
 
 void launch_split_b(const double *B, long ldb, int K, int N, const int32_t *ec, int b, int s, int KC, int n_kc,
                     int BN, int Np, uint16_t *tiles, void *stream, bool trans) {
     const int Kp = n_kc * KC;
     dim3 grid((Np + 31) / 32, (Kp / 8 + 7) / 8);
-    k_split_b<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(B, ldb, K, N, ec, b, s, KC, n_kc, BN, Np,
-                                                                    tiles, trans ? 1 : 0);
+#define OZ_CALL_B(BB)                                                                                    \
+    k_split_b<BB><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(B, ldb, K, N, ec, s, KC, n_kc, BN, Np, tiles, \
+                                                                        trans ? 1 : 0)
+    OZ_SPLIT_DISPATCH(b, OZ_CALL_B)
+#undef OZ_CALL_B
 }
 
 int launch_selftest_timeout(int *err, unsigned long long timeout_ns, void *stream) {
