@@ -66,12 +66,13 @@ struct ozgb_context {
     Plan last{};
     bool have_last = false;
     // buffers
-    DevBuf a, b, c, at, bt, er, ec, ssr, ssc, err, raw, knob, kca, krb, ktmp;
+    DevBuf a, b, c, at, bt, er, ec, err, raw, knob, kpart;
+    KnobJob kjob{};  // the last stage-(a) statistics, for the precision knob
     DevBuf gstat, gslice, gtab;  // grouped calls: statistics, slice planes, job/problem tables
     cudaStream_t stream = nullptr;       // used by the host-array entry points
     // grouped calls: the per-problem GEMMs run on auxiliary streams forked from
     // and joined back into the caller's stream
-    static constexpr int kAux = 8;
+    static constexpr int kAux = 16;
     cudaStream_t aux[kAux] = {};
     cudaEvent_t ev_fork = nullptr;
     cudaEvent_t ev_join[kAux] = {};
@@ -170,29 +171,92 @@ struct Operands {
     double alpha = 1.0, beta = 0.0;
 };
 
-// Stage (a): exponents (+ sums of squares when the precision knob needs them).
+// Statistics layout of one operand pass (launch_stats2d on a rows x cols matrix):
+// partials of its rows at p, of its columns after them.
+struct StatsLayout {
+    size_t row_n, col_n;  // entries
+    int rparts, cparts;
+};
+StatsLayout stats_layout(int rows, int cols) {
+    StatsLayout l;
+    l.rparts = (cols + kStatsCols - 1) / kStatsCols;
+    l.cparts = (rows + kStatsRows - 1) / kStatsRows;
+    l.row_n = static_cast<size_t>(rows) * l.rparts;
+    l.col_n = static_cast<size_t>(l.cparts) * cols;
+    return l;
+}
+StatParts row_parts(const unsigned long long *p, int rows, const StatsLayout &l) {
+    return StatParts{p, rows, l.rparts, l.rparts, 1};
+}
+StatParts col_parts(const unsigned long long *p, int cols, const StatsLayout &l) {
+    return StatParts{p + l.row_n, cols, l.cparts, 1, cols};
+}
+
+// The knob's inputs for op(A) (M x K) and op(B) (K x N) whose stored operands
+// have had launch_stats2d run into pa / pb (rows x cols as stored).
+KnobJob knob_job(const Operands &o, const int32_t *er, const int32_t *ec, const unsigned long long *pa,
+                 const unsigned long long *pb) {
+    KnobJob j{};
+    j.er = er;
+    j.M = o.M;
+    j.ec = ec;
+    j.N = o.N;
+    j.K = o.K;
+    if (!o.ta) {  // A stored M x K: its rows are op(A)'s rows, its columns the k units
+        const StatsLayout la = stats_layout(o.M, o.K);
+        j.ra = row_parts(pa, o.M, la);
+        j.ka = col_parts(pa, o.K, la);
+    } else {  // A stored K x M
+        const StatsLayout la = stats_layout(o.K, o.M);
+        j.ka = row_parts(pa, o.K, la);
+        j.ra = col_parts(pa, o.M, la);
+    }
+    if (!o.tb) {  // B stored K x N: its rows are the k units, its columns op(B)'s columns
+        const StatsLayout lb = stats_layout(o.K, o.N);
+        j.kb = row_parts(pb, o.K, lb);
+        j.cb = col_parts(pb, o.N, lb);
+    } else {  // B stored N x K
+        const StatsLayout lb = stats_layout(o.N, o.K);
+        j.cb = row_parts(pb, o.N, lb);
+        j.kb = col_parts(pb, o.K, lb);
+    }
+    return j;
+}
+
+size_t stats_entries(int rows, int cols) {
+    const StatsLayout l = stats_layout(rows, cols);
+    return l.row_n + l.col_n;
+}
+
+// Stage (a): exponents; when the precision knob needs them, one fused pass per
+// operand also leaves the partial sums of squares of its rows and columns.
 ozgb_status enqueue_exponents(ozgb_handle h, const Operands &o, bool want_ss, cudaStream_t st) {
     if (!h->er.ensure(sizeof(int32_t) * o.M) || !h->ec.ensure(sizeof(int32_t) * o.N))
         return fail(h, OZGB_ERR_ALLOC, "exponent buffers");
-    double *ssr = nullptr, *ssc = nullptr;
-    if (want_ss) {
-        if (!h->ssr.ensure(sizeof(double) * o.M) || !h->ssc.ensure(sizeof(double) * o.N))
-            return fail(h, OZGB_ERR_ALLOC, "statistics buffers");
-        ssr = static_cast<double *>(h->ssr.p);
-        ssc = static_cast<double *>(h->ssc.p);
-        cudaMemsetAsync(ssc, 0, sizeof(double) * o.N, st);
-    }
-    cudaMemsetAsync(h->ec.p, 0, sizeof(int32_t) * o.N, st);
     int32_t *er = static_cast<int32_t *>(h->er.p), *ec = static_cast<int32_t *>(h->ec.p);
-    if (o.ta) {
+    cudaMemsetAsync(ec, 0, sizeof(int32_t) * o.N, st);
+    if (want_ss) {
+        const int ar = o.ta ? o.K : o.M, ac = o.ta ? o.M : o.K;  // A as stored
+        const int br = o.tb ? o.N : o.K, bc = o.tb ? o.K : o.N;  // B as stored
+        const size_t na = stats_entries(ar, ac), nb = stats_entries(br, bc);
+        if (!h->kpart.ensure(sizeof(unsigned long long) * (na + nb)))
+            return fail(h, OZGB_ERR_ALLOC, "statistics buffers");
+        unsigned long long *pa = static_cast<unsigned long long *>(h->kpart.p), *pb = pa + na;
         cudaMemsetAsync(er, 0, sizeof(int32_t) * o.M, st);
-        if (ssr) cudaMemsetAsync(ssr, 0, sizeof(double) * o.M, st);
-        launch_colmax(o.A, o.lda, o.K, o.M, er, ssr, st);  // rows of op(A) are columns of A
+        const StatsLayout la = stats_layout(ar, ac), lb = stats_layout(br, bc);
+        launch_stats2d(o.A, o.lda, ar, ac, o.ta ? nullptr : er, o.ta ? er : nullptr, pa, pa + la.row_n, st);
+        launch_stats2d(o.B, o.ldb, br, bc, o.tb ? ec : nullptr, o.tb ? nullptr : ec, pb, pb + lb.row_n, st);
+        h->kjob = knob_job(o, er, ec, pa, pb);
+    } else if (o.ta) {
+        cudaMemsetAsync(er, 0, sizeof(int32_t) * o.M, st);
+        launch_colmax(o.A, o.lda, o.K, o.M, er, nullptr, st);  // rows of op(A) are columns of A
     } else {
-        launch_rowmax(o.A, o.lda, o.M, o.K, er, ssr, st);
+        launch_rowmax(o.A, o.lda, o.M, o.K, er, nullptr, st);
     }
-    if (o.tb) launch_rowmax(o.B, o.ldb, o.N, o.K, ec, ssc, st);  // columns of op(B) are rows of B
-    else launch_colmax(o.B, o.ldb, o.K, o.N, ec, ssc, st);
+    if (!want_ss) {
+        if (o.tb) launch_rowmax(o.B, o.ldb, o.N, o.K, ec, nullptr, st);  // columns of op(B) are rows of B
+        else launch_colmax(o.B, o.ldb, o.K, o.N, ec, nullptr, st);
+    }
     h->launches += 2;
     return OZGB_OK;
 }
@@ -200,26 +264,13 @@ ozgb_status enqueue_exponents(ozgb_handle h, const Operands &o, bool want_ss, cu
 ozgb_status choose_config(ozgb_handle h, const Operands &o, int mode, cudaStream_t st, OzConfig *cfg) {
     *cfg = resolve_config(h, o.K, mode);
     if (h->err_bound > 0.0 && h->opt_slices <= 0) {
-        // precision knob: besides the stage-(a) row/column statistics it needs the
-        // sums of squares along k (columns of A, rows of B), which two more passes
-        // of the same reduction kernels give; everything is reduced on the device to
+        // precision knob: the stage-(a) partial sums are reduced on the device to
         // five scaled sums, and only those cross to the host
-        if (!h->knob.ensure(5 * sizeof(double)) || !h->kca.ensure(sizeof(double) * o.K) ||
-            !h->krb.ensure(sizeof(double) * o.K) || !h->ktmp.ensure(sizeof(int32_t) * o.K))
-            return fail(h, OZGB_ERR_ALLOC, "knob buffers");
-        double *ca = static_cast<double *>(h->kca.p), *rb = static_cast<double *>(h->krb.p);
-        int32_t *tmp = static_cast<int32_t *>(h->ktmp.p);
-        cudaMemsetAsync(ca, 0, sizeof(double) * o.K, st);
-        cudaMemsetAsync(tmp, 0, sizeof(int32_t) * o.K, st);
-        // ca[k] = |op(A)(:,k)|^2, rb[k] = |op(B)(k,:)|^2
-        if (o.ta) launch_rowmax(o.A, o.lda, o.K, o.M, tmp, ca, st);
-        else launch_colmax(o.A, o.lda, o.M, o.K, tmp, ca, st);
-        if (o.tb) launch_colmax(o.B, o.ldb, o.N, o.K, tmp, rb, st);
-        else launch_rowmax(o.B, o.ldb, o.K, o.N, tmp, rb, st);
-        launch_knob_stats(static_cast<int32_t *>(h->er.p), static_cast<double *>(h->ssr.p), o.M,
-                          static_cast<int32_t *>(h->ec.p), static_cast<double *>(h->ssc.p), o.N, ca, rb, o.K,
-                          static_cast<double *>(h->knob.p), st);
-        h->launches += 3;
+        if (!h->knob.ensure(5 * sizeof(double))) return fail(h, OZGB_ERR_ALLOC, "knob buffer");
+        KnobJob j = h->kjob;
+        j.out = static_cast<double *>(h->knob.p);
+        launch_knob_stats(j, st);
+        h->launches += 1;
         KnobStats ks;
         cudaMemcpyAsync(&ks, h->knob.p, sizeof ks, cudaMemcpyDeviceToHost, st);
         cudaError_t e = cudaStreamSynchronize(st);
@@ -460,10 +511,11 @@ ozgb_status enqueue_grouped(ozgb_handle h, ozgb_problem *probs, int n, int mode,
         bound[i] = bd > 0.0 ? bd : 0.0;
         if (bound[i] > 0.0) adapt_idx[i] = n_adapt++;
     }
-    // ---- statistics scratch: er, ec (int32); ssr, ssc, ca, rb (double) when
-    // adaptive; the knob outputs of all adaptive problems contiguous at the end
+    // ---- statistics scratch: er, ec (int32); for adaptive problems the partial
+    // sums of squares of A's and B's rows and columns; the knob outputs of all
+    // adaptive problems contiguous at the end
     struct StatOff {
-        size_t er, ec, ssr, ssc, ca, rb;
+        size_t er, ec, pa, pb;
     };
     std::vector<StatOff> so(n);
     size_t total = 0;
@@ -475,14 +527,10 @@ ozgb_status enqueue_grouped(ozgb_handle h, ozgb_problem *probs, int n, int mode,
         so[i].ec = total;
         total += align256(sizeof(int32_t) * pb.N);
         if (bound[i] > 0.0) {
-            so[i].ssr = total;
-            total += align256(sizeof(double) * pb.M);
-            so[i].ssc = total;
-            total += align256(sizeof(double) * pb.N);
-            so[i].ca = total;
-            total += align256(sizeof(double) * pb.K);
-            so[i].rb = total;
-            total += align256(sizeof(double) * pb.K);
+            so[i].pa = total;
+            total += align256(sizeof(unsigned long long) * stats_entries(pb.M, pb.K));
+            so[i].pb = total;
+            total += align256(sizeof(unsigned long long) * stats_entries(pb.K, pb.N));
         }
     }
     const size_t knob_off = total;
@@ -522,31 +570,31 @@ ozgb_status enqueue_grouped(ozgb_handle h, ozgb_problem *probs, int n, int mode,
     const KnobJob *dkj = nullptr;
     for (int i = 0; i < n; ++i) {
         const ozgb_problem &pb = probs[i];
-        const bool ad = bound[i] > 0.0;
+        int32_t *er = reinterpret_cast<int32_t *>(at(so[i].er)), *ec = reinterpret_cast<int32_t *>(at(so[i].ec));
         StageJob j{};
-        j.kind = JOB_ROWMAX, j.X = pb.A, j.ld = pb.lda, j.rows = pb.M, j.cols = pb.K;
-        j.e_out = reinterpret_cast<int32_t *>(at(so[i].er));
-        j.ss_out = ad ? reinterpret_cast<double *>(at(so[i].ssr)) : nullptr;
-        ja.add(j);
-        j = StageJob{};
-        j.kind = JOB_COLMAX, j.X = pb.B, j.ld = pb.ldb, j.rows = pb.K, j.cols = pb.N;
-        j.e_out = reinterpret_cast<int32_t *>(at(so[i].ec));
-        j.ss_out = ad ? reinterpret_cast<double *>(at(so[i].ssc)) : nullptr;
-        ja.add(j);
-        if (ad) {
-            j = StageJob{};
-            j.kind = JOB_COLMAX, j.X = pb.A, j.ld = pb.lda, j.rows = pb.M, j.cols = pb.K;
-            j.ss_out = reinterpret_cast<double *>(at(so[i].ca));
+        if (bound[i] > 0.0) {
+            // one pass per operand: exponents and the partial sums of squares
+            unsigned long long *pa = reinterpret_cast<unsigned long long *>(at(so[i].pa));
+            unsigned long long *pbp = reinterpret_cast<unsigned long long *>(at(so[i].pb));
+            j.kind = JOB_STATS, j.X = pb.A, j.ld = pb.lda, j.rows = pb.M, j.cols = pb.K;
+            j.e_out = er, j.e_out2 = nullptr, j.prow = pa, j.pcol = pa + stats_layout(pb.M, pb.K).row_n;
             ja.add(j);
             j = StageJob{};
-            j.kind = JOB_ROWMAX, j.X = pb.B, j.ld = pb.ldb, j.rows = pb.K, j.cols = pb.N;
-            j.ss_out = reinterpret_cast<double *>(at(so[i].rb));
+            j.kind = JOB_STATS, j.X = pb.B, j.ld = pb.ldb, j.rows = pb.K, j.cols = pb.N;
+            j.e_out = nullptr, j.e_out2 = ec, j.prow = pbp, j.pcol = pbp + stats_layout(pb.K, pb.N).row_n;
             ja.add(j);
-            kj.push_back(KnobJob{reinterpret_cast<int32_t *>(at(so[i].er)), reinterpret_cast<double *>(at(so[i].ssr)),
-                                 pb.M, reinterpret_cast<int32_t *>(at(so[i].ec)),
-                                 reinterpret_cast<double *>(at(so[i].ssc)), pb.N,
-                                 reinterpret_cast<double *>(at(so[i].ca)), reinterpret_cast<double *>(at(so[i].rb)),
-                                 pb.K, reinterpret_cast<double *>(knob_dev + adapt_idx[i])});
+            Operands op{pb.M, pb.N, pb.K, pb.A, pb.lda, pb.B, pb.ldb, pb.C, pb.ldc};
+            KnobJob kjb = knob_job(op, er, ec, pa, pbp);
+            kjb.out = reinterpret_cast<double *>(knob_dev + adapt_idx[i]);
+            kj.push_back(kjb);
+        } else {
+            j.kind = JOB_ROWMAX, j.X = pb.A, j.ld = pb.lda, j.rows = pb.M, j.cols = pb.K;
+            j.e_out = er;
+            ja.add(j);
+            j = StageJob{};
+            j.kind = JOB_COLMAX, j.X = pb.B, j.ld = pb.ldb, j.rows = pb.K, j.cols = pb.N;
+            j.e_out = ec;
+            ja.add(j);
         }
     }
     ja.block0.push_back(ja.total);
@@ -724,8 +772,8 @@ ozgb_status ozgb_release(ozgb_handle h) {
     if (!h) return OZGB_ERR_ARG;
     std::lock_guard<std::mutex> lk(h->mu);
     if (h->device >= 0) cudaSetDevice(h->device);
-    for (DevBuf *b : {&h->a, &h->b, &h->c, &h->at, &h->bt, &h->er, &h->ec, &h->ssr, &h->ssc, &h->raw, &h->knob, &h->kca,
-                      &h->krb, &h->ktmp, &h->gstat, &h->gslice, &h->gtab})
+    for (DevBuf *b : {&h->a, &h->b, &h->c, &h->at, &h->bt, &h->er, &h->ec, &h->raw, &h->knob, &h->kpart, &h->gstat,
+                      &h->gslice, &h->gtab})
         b->release();
     // captured grouped graphs refer to the released buffers
     if (h->gexec1) cudaGraphExecDestroy(h->gexec1);

@@ -76,35 +76,49 @@ struct GemmArgs {
     double alpha, beta;  // C = alpha * (A B) + beta * C for OUT_RN / OUT_RZ_REF (1, 0: plain store)
 };
 
+// Partial sums of squares of reduction units (rows or columns of an operand),
+// packed as (E << 32) | float_bits(s): s = sum of (x / 2^(E-1023))^2 over one
+// slab of the unit, E the slab's largest exponent field (zeros and subnormals
+// contribute nothing).  FP32 with a running exponent keeps FP64 arithmetic, slow
+// on GB300, out of the pass over the operands.  The partials of unit u are at
+// p[u * unit_stride + i * part_stride], i < nparts.
+struct StatParts {
+    const unsigned long long *p;
+    int n_units, nparts;
+    long unit_stride, part_stride;
+};
+
 // Work items of the grouped stage-(a)/(b) launch (k_stage_jobs): each job is one
 // of the per-problem kernels below, run on blocks [block0, block0 + gx * gy) of
 // the launch with local block coordinates (bx, by).
-enum StageKind : int { JOB_ROWMAX = 0, JOB_COLMAX = 1, JOB_SPLIT_A = 2, JOB_SPLIT_B = 3 };
+enum StageKind : int { JOB_ROWMAX = 0, JOB_COLMAX = 1, JOB_SPLIT_A = 2, JOB_SPLIT_B = 3, JOB_STATS = 4 };
 struct StageJob {
     int kind, gx, gy;
     const double *X;     // A (M x K) or B (K x N), row-major
     long ld;
     int rows, cols;      // of X
-    int32_t *e_out;      // ROWMAX / COLMAX: exponent fields (may be null)
+    int32_t *e_out;      // ROWMAX / COLMAX / STATS (rows): exponent fields, atomic max for STATS (may be null)
     double *ss_out;      // ROWMAX / COLMAX: sums of squares (may be null)
     const int32_t *e_in; // SPLIT: row (A) / column (B) exponents
     int b, s, KC, n_kc, padded, BN;  // SPLIT: padded = Mp (A) or Np (B)
     uint16_t *tiles;
+    int32_t *e_out2;                  // STATS: column exponent fields (atomic max, may be null)
+    unsigned long long *prow, *pcol;  // STATS: row partials [rows][ceil(cols/256)], column partials [ceil(rows/64)][cols]
 };
 constexpr int kStageThreads = 256;
+constexpr int kStatsCols = 256, kStatsRows = 64;  // STATS tile
 
-// Per-problem inputs of the grouped precision-knob reduction (3 blocks each).
+// Per-problem inputs of the precision-knob reduction: the row exponents of op(A)
+// and column exponents of op(B), and the partial sums of squares of the rows of
+// op(A), columns of op(B), columns of op(A) and rows of op(B) (k units).
 struct KnobJob {
     const int32_t *er;
-    const double *ssr;
     int M;
     const int32_t *ec;
-    const double *ssc;
     int N;
-    const double *ca;
-    const double *rb;
     int K;
-    double *out;  // 5 doubles
+    StatParts ra, cb, ka, kb;
+    double *out;  // 5 doubles, zeroed before
 };
 
 // Device error codes written to the error word.
@@ -131,11 +145,15 @@ void launch_split_a(const double *A, long lda, int M, int K, const int32_t *er, 
 void launch_split_b(const double *B, long ldb, int K, int N, const int32_t *ec, int b, int s, int KC, int n_kc,
                     int BN, int Np, uint16_t *tiles, void *stream, bool trans = false);
 int launch_selftest_timeout(int *err, unsigned long long timeout_ns, void *stream);
-// Precision-knob statistics (five doubles, see KnobStats in oz_plan.h) from the
-// row/column exponents and sums of squares of stage (a) and the per-k sums of
-// squares ca[k] = |A(:,k)|^2, rb[k] = |B(k,:)|^2.
-void launch_knob_stats(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N,
-                       const double *ca, const double *rb, int K, double *out, void *stream);
+// One pass over a row-major rows x cols operand: exponent maxima of its rows
+// and/or columns (atomic max into row_e / col_e, zeroed before; either may be
+// null) and the partial sums of squares of its rows and columns (StatParts
+// layouts: row_part[r * ceil(cols/256) + i], col_part[i * cols + c]).
+void launch_stats2d(const double *X, long ld, int rows, int cols, int32_t *row_e, int32_t *col_e,
+                    unsigned long long *row_part, unsigned long long *col_part, void *stream);
+// Precision-knob statistics (five doubles, see KnobStats in oz_plan.h) of one
+// problem; zeroes j.out first.
+void launch_knob_stats(const KnobJob &j, void *stream);
 // Grid sizes of the per-problem stage kernels (blocks in x and y of 256 threads).
 void stage_grid(const StageJob &j, int *gx, int *gy);
 // Grouped launches: all jobs in one grid (block0[i] = first block of job i,

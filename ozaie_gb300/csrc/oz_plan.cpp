@@ -58,6 +58,7 @@ namespace {
 using TuneKey = std::tuple<int, int, int, int, int, int, int>;
 std::mutex g_tune_mu;
 std::map<TuneKey, PlanHints> g_tune;
+long g_tune_generation = 0;  // bumped whenever the table changes (plans cached under the old one are stale)
 
 int ceil_log2(int x) {
     int l = 0;
@@ -72,6 +73,7 @@ TuneKey tune_key(int M, int N, int K, const OzConfig &cfg) {
 void tune_store(int M, int N, int K, const OzConfig &cfg, const PlanHints &h) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune[tune_key(M, N, K, cfg)] = h;
+    ++g_tune_generation;
 }
 bool tune_lookup(int M, int N, int K, const OzConfig &cfg, PlanHints *h) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -83,14 +85,56 @@ bool tune_lookup(int M, int N, int K, const OzConfig &cfg, PlanHints *h) {
 void tune_clear() {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune.clear();
+    ++g_tune_generation;
 }
 int tune_count() {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     return static_cast<int>(g_tune.size());
 }
 
+namespace {
+bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string *err, int bin_lo, int bin_hi,
+                        const PlanHints *hints);
+}
+
+namespace {
+// Plans without hints are pure functions of the shape, the configuration and the
+// tuning table: cached, so that grouped calls with many problems plan in O(1) each.
+using PlanKey = std::tuple<int, int, int, int, int, int, int, int, int, long>;
+std::mutex g_plan_mu;
+std::map<PlanKey, Plan> g_plans;
+}  // namespace
+
 bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string *err, int bin_lo, int bin_hi,
                const PlanHints *hints) {
+    if (hints || std::getenv("OZGB_KC") || std::getenv("OZGB_GROUPS"))
+        return make_plan_uncached(M, N, K, cfg, out, err, bin_lo, bin_hi, hints);
+    long gen;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        gen = g_tune_generation;
+    }
+    const PlanKey key{M, N, K, cfg.b, cfg.s, cfg.J, cfg.rounding, bin_lo, std::min(bin_hi, 1 << 20), gen};
+    {
+        std::lock_guard<std::mutex> lk(g_plan_mu);
+        auto it = g_plans.find(key);
+        if (it != g_plans.end()) {
+            *out = it->second;
+            return true;
+        }
+    }
+    Plan p;
+    if (!make_plan_uncached(M, N, K, cfg, &p, err, bin_lo, bin_hi, nullptr)) return false;
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    if (g_plans.size() > 8192) g_plans.clear();
+    g_plans[key] = p;
+    *out = p;
+    return true;
+}
+
+namespace {
+bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string *err, int bin_lo, int bin_hi,
+                        const PlanHints *hints) {
     PlanHints tuned;
     if (!hints && bin_lo <= 0 && bin_hi >= cfg.J - 1 && tune_lookup(M, N, K, cfg, &tuned)) hints = &tuned;
     const PlanHints none;
@@ -382,6 +426,8 @@ bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string 
     *out = p;
     return true;
 }
+
+}  // namespace
 
 std::vector<PlanHints> plan_candidates(int M, int N, int K, const OzConfig &cfg, int max_n) {
     std::vector<PlanHints> out;

@@ -294,63 +294,200 @@ __device__ __forceinline__ double scale2(double x, int e) {
     return x * pow2i(h) * pow2i(e - h);
 }
 
-// Part `chunk` of `chunks` of one of the three sums (role 0: A terms, 1: B
-// terms, 2: the k-direction term), added atomically into out (zeroed before).
-__device__ __forceinline__ void knob_stats_body(const int32_t *__restrict__ er, const double *__restrict__ ssr, int M,
-                                                const int32_t *__restrict__ ec, const double *__restrict__ ssc, int N,
-                                                const double *__restrict__ ca, const double *__restrict__ rb, int K,
-                                                double *__restrict__ out, const int role, const int chunk,
-                                                const int chunks) {
+// ------------------------------------------------ FP32 scaled sums of squares
+// 4^d as a float for d <= 0 (0 below the normal range).
+__device__ __forceinline__ float pow4f(int d) { return d < -63 ? 0.0f : __int_as_float((127 + 2 * d) << 23); }
+
+// (E, s) += the square of x: s is in units of 4^(E-1023), E the largest exponent
+// field seen; x's own mantissa m in [1, 2) squared is added at 4^(e-E).
+__device__ __forceinline__ void sq_add(int &E, float &s, double x) {
+    const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(x));
+    const int e = static_cast<int>((u >> 52) & 0x7FF);
+    if (e == 0 || e == 0x7FF) return;  // zeros and subnormals (negligible); no infinities
+    const float m = __uint_as_float(0x3F800000u | static_cast<uint32_t>((u >> 29) & 0x7FFFFF));
+    if (e > E) {
+        s *= pow4f(E - e);
+        E = e;
+    }
+    s = fmaf(m * m, pow4f(e - E), s);
+}
+__device__ __forceinline__ void sq_merge(int &E, float &s, int E2, float s2) {
+    const int Em = max(E, E2);
+    s = s * pow4f(E - Em) + s2 * pow4f(E2 - Em);
+    E = Em;
+}
+__device__ __forceinline__ unsigned long long sq_pack(int E, float s) {
+    return (static_cast<unsigned long long>(static_cast<uint32_t>(E)) << 32) | __float_as_uint(s);
+}
+
+// (E, s) += m2 * 4^(e - 1023) for an element with exponent field e and squared
+// mantissa m2 (0 for zeros, subnormals and non-finite values).
+__device__ __forceinline__ void sq_add_em(int &E, float &s, int e, float m2) {
+    if (e > E) {
+        s *= pow4f(E - e);
+        E = e;
+    }
+    s = fmaf(m2, pow4f(e - E), s);
+}
+
+// One 64-row x 256-column tile.  Thread t owns column bx*256+t (coalesced row
+// reads, 8 rows in flight); the rows are reduced through shared memory 8 rows
+// at a time, one warp per row.
+__device__ __forceinline__ void stats2d_body(const double *__restrict__ X, long ld, int rows, int cols,
+                                             int32_t *__restrict__ row_e, int32_t *__restrict__ col_e,
+                                             unsigned long long *__restrict__ row_part,
+                                             unsigned long long *__restrict__ col_part, int bx, int by) {
+    constexpr int RB = kStageThreads / 32;  // rows per chunk = warps per block
+    __shared__ int shE[RB][kStatsCols];
+    __shared__ float shM[RB][kStatsCols];
+    __shared__ int rE[kStatsRows];
+    __shared__ float rS[kStatsRows];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int c = bx * kStatsCols + threadIdx.x;
+    const int r0 = by * kStatsRows;
+    const bool cin = c < cols;
+    const bool rows_wanted = row_e || row_part;
+    int Ec = 0;
+    float sc = 0.0f;
+    for (int i0 = 0; i0 < kStatsRows; i0 += RB) {
+        double x[RB];
+#pragma unroll
+        for (int u = 0; u < RB; ++u) {
+            const int r = r0 + i0 + u;
+            x[u] = (cin && r < rows) ? __ldg(X + static_cast<size_t>(r) * ld + c) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < RB; ++u) {
+            const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(x[u]));
+            const int e = static_cast<int>((bits >> 52) & 0x7FF);
+            float m2 = 0.0f;
+            if (e != 0 && e != 0x7FF) {
+                const float m = __uint_as_float(0x3F800000u | static_cast<uint32_t>((bits >> 29) & 0x7FFFFF));
+                m2 = m * m;
+            }
+            sq_add_em(Ec, sc, e, m2);
+            if (rows_wanted) {
+                shE[u][threadIdx.x] = e;
+                shM[u][threadIdx.x] = m2;
+            }
+        }
+        if (rows_wanted) {
+            __syncthreads();
+            int E = 0;
+            float sr = 0.0f;
+            for (int q = lane; q < kStatsCols; q += 32) sq_merge(E, sr, shE[wid][q], shM[wid][q]);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const int e2 = __shfl_xor_sync(0xffffffffu, E, o);
+                const float s2 = __shfl_xor_sync(0xffffffffu, sr, o);
+                sq_merge(E, sr, e2, s2);
+            }
+            if (lane == 0) {
+                rE[i0 + wid] = E;
+                rS[i0 + wid] = sr;
+            }
+            __syncthreads();
+        }
+    }
+    if (rows_wanted) {
+        const int r = r0 + static_cast<int>(threadIdx.x);
+        if (threadIdx.x < kStatsRows && r < rows) {
+            if (row_part)
+                row_part[static_cast<size_t>(r) * ((cols + kStatsCols - 1) / kStatsCols) + bx] =
+                    sq_pack(rE[threadIdx.x], rS[threadIdx.x]);
+            if (row_e) atomicMax(row_e + r, rE[threadIdx.x]);
+        }
+    }
+    if (cin) {
+        if (col_part) col_part[static_cast<size_t>(by) * cols + c] = sq_pack(Ec, sc);
+        if (col_e) atomicMax(col_e + c, Ec);
+    }
+}
+
+__global__ void __launch_bounds__(kStageThreads) k_stats2d(const double *__restrict__ X, long ld, int rows, int cols,
+                                                           int32_t *row_e, int32_t *col_e, unsigned long long *row_part,
+                                                           unsigned long long *col_part) {
+    stats2d_body(X, ld, rows, cols, row_e, col_e, row_part, col_part, blockIdx.x, blockIdx.y);
+}
+
+void launch_stats2d(const double *X, long ld, int rows, int cols, int32_t *row_e, int32_t *col_e,
+                    unsigned long long *row_part, unsigned long long *col_part, void *stream) {
+    dim3 grid((cols + kStatsCols - 1) / kStatsCols, (rows + kStatsRows - 1) / kStatsRows);
+    k_stats2d<<<grid, kStageThreads, 0, static_cast<cudaStream_t>(stream)>>>(X, ld, rows, cols, row_e, col_e, row_part,
+                                                                              col_part);
+}
+
+// Combined (E, s) of unit u, and its sum of squares scaled by 4^(shift).
+__device__ __forceinline__ void unit_sq(const StatParts &sp, int u, int *E, float *s) {
+    int e = 0;
+    float v = 0.0f;
+    const unsigned long long *p = sp.p + u * sp.unit_stride;
+    for (int i = 0; i < sp.nparts; ++i) {
+        const unsigned long long w = p[i * sp.part_stride];
+        sq_merge(e, v, static_cast<int>(w >> 32), __uint_as_float(static_cast<uint32_t>(w)));
+    }
+    *E = e;
+    *s = v;
+}
+
+// Part `chunk` of `chunks` of one of the three knob sums (role 0: A terms, 1: B
+// terms, 2: the k-direction term), added atomically into j.out (zeroed before).
+// With ea, eb the largest row / column exponents of op(A) / op(B):
+//   sa = sum_r 4^(Er - ea), na = sum_r |a_r|^2 4^(1022 - ea), likewise for B,
+//   t  = sum_k |op(A)(:,k)|^2 |op(B)(k,:)|^2 4^(2044 - ea - eb).
+__device__ __forceinline__ void knob_stats_body(const KnobJob &j, const int role, const int chunk, const int chunks) {
     __shared__ int sh_i[32];
     __shared__ double sh_d[32];
     int ea = 0, eb = 0;
     if (role != 1) {
-        for (int i = threadIdx.x; i < M; i += blockDim.x) ea = max(ea, er[i]);
+        for (int i = threadIdx.x; i < j.M; i += blockDim.x) ea = max(ea, j.er[i]);
         ea = block_max_int(ea, sh_i);
     }
     if (role != 0) {
-        for (int j = threadIdx.x; j < N; j += blockDim.x) eb = max(eb, ec[j]);
+        for (int i = threadIdx.x; i < j.N; i += blockDim.x) eb = max(eb, j.ec[i]);
         eb = block_max_int(eb, sh_i);
     }
-    const int n = role == 0 ? M : (role == 1 ? N : K);
+    const int n = role == 0 ? j.M : (role == 1 ? j.N : j.K);
     const int per = (n + chunks - 1) / chunks;
     const int i0 = chunk * per, i1 = min(n, i0 + per);
     if (role < 2) {
-        const int32_t *e = role == 0 ? er : ec;
-        const double *ss = role == 0 ? ssr : ssc;
+        const int32_t *e = role == 0 ? j.er : j.ec;
+        const StatParts &sp = role == 0 ? j.ra : j.cb;
         const int emax = role == 0 ? ea : eb;
         double num = 0.0, den = 0.0;
         for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+            int E;
+            float sq;
+            unit_sq(sp, i, &E, &sq);
             num += pow2i(2 * (e[i] - emax));
-            den += scale2(ss[i], -2 * (emax - 1022));
+            den += scale2(static_cast<double>(sq), 2 * (E - emax) - 2);
         }
         num = block_sum(num, sh_d);
         den = block_sum(den, sh_d);
         if (threadIdx.x == 0) {
-            atomicAdd(out + 2 * role, num);
-            atomicAdd(out + 2 * role + 1, den);
+            atomicAdd(j.out + 2 * role, num);
+            atomicAdd(j.out + 2 * role + 1, den);
         }
     } else {
         double t = 0.0;
-        for (int k = i0 + threadIdx.x; k < i1; k += blockDim.x)
-            t += scale2(ca[k], -2 * (ea - 1022)) * scale2(rb[k], -2 * (eb - 1022));
+        for (int k = i0 + threadIdx.x; k < i1; k += blockDim.x) {
+            int E1, E2;
+            float s1, s2;
+            unit_sq(j.ka, k, &E1, &s1);
+            unit_sq(j.kb, k, &E2, &s2);
+            t += scale2(static_cast<double>(s1) * s2, 2 * (E1 + E2 - ea - eb - 2));
+        }
         t = block_sum(t, sh_d);
-        if (threadIdx.x == 0) atomicAdd(out + 4, t);
+        if (threadIdx.x == 0) atomicAdd(j.out + 4, t);
     }
 }
 
-// ---------------------------------------------------------------- launches
-__global__ void k_knob_stats(const int32_t *__restrict__ er, const double *__restrict__ ssr, int M,
-                             const int32_t *__restrict__ ec, const double *__restrict__ ssc, int N,
-                             const double *__restrict__ ca, const double *__restrict__ rb, int K,
-                             double *__restrict__ out) {
-    knob_stats_body(er, ssr, M, ec, ssc, N, ca, rb, K, out, blockIdx.x % 3, blockIdx.x / 3, gridDim.x / 3);
-}
+__global__ void k_knob_stats(const KnobJob j) { knob_stats_body(j, blockIdx.x % 3, blockIdx.x / 3, gridDim.x / 3); }
 
 // Grouped knob reduction: blocks 3p, 3p+1, 3p+2 reduce problem p.
 __global__ void k_knob_grouped(const KnobJob *__restrict__ jobs) {
     const KnobJob j = jobs[blockIdx.x / 3];
-    knob_stats_body(j.er, j.ssr, j.M, j.ec, j.ssc, j.N, j.ca, j.rb, j.K, j.out, blockIdx.x % 3, 0, 1);
+    knob_stats_body(j, blockIdx.x % 3, 0, 1);
 }
 
 // Grouped stage (a)/(b): block -> job by binary search over block0[], then the
@@ -370,6 +507,7 @@ __global__ void __launch_bounds__(kStageThreads) k_stage_jobs(const StageJob *__
     switch (j.kind) {
         case JOB_ROWMAX: rowmax_body(j.X, j.ld, j.rows, j.cols, j.e_out, j.ss_out, bx, by); break;
         case JOB_COLMAX: colmax_body(j.X, j.ld, j.rows, j.cols, 64, j.e_out, j.ss_out, bx, by); break;
+        case JOB_STATS: stats2d_body(j.X, j.ld, j.rows, j.cols, j.e_out, j.e_out2, j.prow, j.pcol, bx, by); break;
         case JOB_SPLIT_A: {
 #define OZ_JOB_A(BB) split_a_body<BB>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.padded, j.tiles, bx, by, false)
             OZ_SPLIT_DISPATCH(j.b, OZ_JOB_A)
@@ -428,6 +566,10 @@ void stage_grid(const StageJob &j, int *gx, int *gy) {
             *gx = (j.cols + kStageThreads - 1) / kStageThreads;
             *gy = (j.rows + 63) / 64;
             break;
+        case JOB_STATS:
+            *gx = (j.cols + kStatsCols - 1) / kStatsCols;
+            *gy = (j.rows + kStatsRows - 1) / kStatsRows;
+            break;
         case JOB_SPLIT_A:
             *gx = (j.n_kc * j.KC / 8 + 31) / 32;
             *gy = j.padded / 8;
@@ -448,12 +590,11 @@ void launch_knob_grouped(const KnobJob *jobs, int n, void *stream) {
     if (n > 0) k_knob_grouped<<<3 * n, 1024, 0, static_cast<cudaStream_t>(stream)>>>(jobs);
 }
 
-void launch_knob_stats(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N,
-                       const double *ca, const double *rb, int K, double *out, void *stream) {
+void launch_knob_stats(const KnobJob &j, void *stream) {
     // each of the three sums split over up to 32 blocks of 256 threads
-    const int chunks = std::max(1, std::min(32, std::max(M, std::max(N, K)) / 1024));
-    cudaMemsetAsync(out, 0, 5 * sizeof(double), static_cast<cudaStream_t>(stream));
-    k_knob_stats<<<3 * chunks, 256, 0, static_cast<cudaStream_t>(stream)>>>(er, ssr, M, ec, ssc, N, ca, rb, K, out);
+    const int chunks = std::max(1, std::min(32, std::max(j.M, std::max(j.N, j.K)) / 1024));
+    cudaMemsetAsync(j.out, 0, 5 * sizeof(double), static_cast<cudaStream_t>(stream));
+    k_knob_stats<<<3 * chunks, 256, 0, static_cast<cudaStream_t>(stream)>>>(j);
 }
 
 void launch_rowmax(const double *A, long lda, int M, int K, int32_t *er, double *ss, void *stream) {
