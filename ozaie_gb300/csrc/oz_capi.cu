@@ -72,7 +72,7 @@ struct ozgb_context {
     cudaStream_t stream = nullptr;       // used by the host-array entry points
     // grouped calls: the per-problem GEMMs run on auxiliary streams forked from
     // and joined back into the caller's stream
-    static constexpr int kAux = 16;
+    static constexpr int kAux = 32;
     cudaStream_t aux[kAux] = {};
     cudaEvent_t ev_fork = nullptr;
     cudaEvent_t ev_join[kAux] = {};
