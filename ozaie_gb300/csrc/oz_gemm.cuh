@@ -752,7 +752,19 @@ inline int device_sm_count() {
 template <int BN, int W, int KC>
 void launch_gemm_variant(const GemmArgs &args, int tiles, size_t smem, void *stream) {
     auto kern = oz_gemm_kernel<BN, W, KC>;
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    // the shared-memory limit is raised once per device to the opt-in maximum (a
+    // per-launch attribute call costs more than the launch itself; every caller
+    // sets the same value, so concurrent first calls do not conflict)
+    static bool raised[64] = {false};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64 || !raised[dev]) {
+        int opt = 0;
+        cudaDeviceGetAttribute(&opt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             opt > static_cast<int>(smem) ? opt : static_cast<int>(smem));
+        if (dev >= 0 && dev < 64) raised[dev] = true;
+    }
     const int grid = args.total_tiles < device_sm_count() ? args.total_tiles : device_sm_count();
     (void)tiles;
     kern<<<grid, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(args);

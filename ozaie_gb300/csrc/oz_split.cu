@@ -417,27 +417,36 @@ void launch_stats2d(const double *X, long ld, int rows, int cols, int32_t *row_e
                                                                               col_part);
 }
 
-// Combined (E, s) of unit u, and its sum of squares scaled by 4^(shift).
-__device__ __forceinline__ void unit_sq(const StatParts &sp, int u, int *E, float *s) {
+// Combined (E, s) of unit u, by one warp: lanes load the unit's partials in
+// parallel and merge them; every lane returns the result.
+__device__ __forceinline__ void unit_sq_warp(const StatParts &sp, int u, int lane, int *E, float *s) {
     int e = 0;
     float v = 0.0f;
     const unsigned long long *p = sp.p + u * sp.unit_stride;
-    for (int i = 0; i < sp.nparts; ++i) {
-        const unsigned long long w = p[i * sp.part_stride];
+    for (int i = lane; i < sp.nparts; i += 32) {
+        const unsigned long long w = __ldg(p + i * sp.part_stride);
         sq_merge(e, v, static_cast<int>(w >> 32), __uint_as_float(static_cast<uint32_t>(w)));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const int e2 = __shfl_xor_sync(0xffffffffu, e, o);
+        const float v2 = __shfl_xor_sync(0xffffffffu, v, o);
+        sq_merge(e, v, e2, v2);
     }
     *E = e;
     *s = v;
 }
 
 // Part `chunk` of `chunks` of one of the three knob sums (role 0: A terms, 1: B
-// terms, 2: the k-direction term), added atomically into j.out (zeroed before).
-// With ea, eb the largest row / column exponents of op(A) / op(B):
+// terms, 2: the k-direction term), added atomically into j.out (zeroed before);
+// one warp per unit.  With ea, eb the largest row / column exponents of op(A) /
+// op(B):
 //   sa = sum_r 4^(Er - ea), na = sum_r |a_r|^2 4^(1022 - ea), likewise for B,
 //   t  = sum_k |op(A)(:,k)|^2 |op(B)(k,:)|^2 4^(2044 - ea - eb).
 __device__ __forceinline__ void knob_stats_body(const KnobJob &j, const int role, const int chunk, const int chunks) {
     __shared__ int sh_i[32];
     __shared__ double sh_d[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     int ea = 0, eb = 0;
     if (role != 1) {
         for (int i = threadIdx.x; i < j.M; i += blockDim.x) ea = max(ea, j.er[i]);
@@ -450,18 +459,27 @@ __device__ __forceinline__ void knob_stats_body(const KnobJob &j, const int role
     const int n = role == 0 ? j.M : (role == 1 ? j.N : j.K);
     const int per = (n + chunks - 1) / chunks;
     const int i0 = chunk * per, i1 = min(n, i0 + per);
-    if (role < 2) {
-        const int32_t *e = role == 0 ? j.er : j.ec;
-        const StatParts &sp = role == 0 ? j.ra : j.cb;
-        const int emax = role == 0 ? ea : eb;
-        double num = 0.0, den = 0.0;
-        for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    double num = 0.0, den = 0.0, t = 0.0;
+    for (int u = i0 + wid; u < i1; u += nw) {
+        if (role < 2) {
+            const StatParts &sp = role == 0 ? j.ra : j.cb;
+            const int emax = role == 0 ? ea : eb;
             int E;
             float sq;
-            unit_sq(sp, i, &E, &sq);
-            num += pow2i(2 * (e[i] - emax));
-            den += scale2(static_cast<double>(sq), 2 * (E - emax) - 2);
+            unit_sq_warp(sp, u, lane, &E, &sq);
+            if (lane == 0) {
+                num += pow2i(2 * ((role == 0 ? j.er[u] : j.ec[u]) - emax));
+                den += scale2(static_cast<double>(sq), 2 * (E - emax) - 2);
+            }
+        } else {
+            int E1, E2;
+            float s1, s2;
+            unit_sq_warp(j.ka, u, lane, &E1, &s1);
+            unit_sq_warp(j.kb, u, lane, &E2, &s2);
+            if (lane == 0) t += scale2(static_cast<double>(s1) * s2, 2 * (E1 + E2 - ea - eb - 2));
         }
+    }
+    if (role < 2) {
         num = block_sum(num, sh_d);
         den = block_sum(den, sh_d);
         if (threadIdx.x == 0) {
@@ -469,14 +487,6 @@ __device__ __forceinline__ void knob_stats_body(const KnobJob &j, const int role
             atomicAdd(j.out + 2 * role + 1, den);
         }
     } else {
-        double t = 0.0;
-        for (int k = i0 + threadIdx.x; k < i1; k += blockDim.x) {
-            int E1, E2;
-            float s1, s2;
-            unit_sq(j.ka, k, &E1, &s1);
-            unit_sq(j.kb, k, &E2, &s2);
-            t += scale2(static_cast<double>(s1) * s2, 2 * (E1 + E2 - ea - eb - 2));
-        }
         t = block_sum(t, sh_d);
         if (threadIdx.x == 0) atomicAdd(j.out + 4, t);
     }
@@ -591,8 +601,8 @@ void launch_knob_grouped(const KnobJob *jobs, int n, void *stream) {
 }
 
 void launch_knob_stats(const KnobJob &j, void *stream) {
-    // each of the three sums split over up to 32 blocks of 256 threads
-    const int chunks = std::max(1, std::min(32, std::max(j.M, std::max(j.N, j.K)) / 1024));
+    // each of the three sums split over blocks of 8 warps, about 64 units per block
+    const int chunks = std::max(1, std::min(1024, std::max(j.M, std::max(j.N, j.K)) / 64));
     cudaMemsetAsync(j.out, 0, 5 * sizeof(double), static_cast<cudaStream_t>(stream));
     k_knob_stats<<<3 * chunks, 256, 0, static_cast<cudaStream_t>(stream)>>>(j);
 }
