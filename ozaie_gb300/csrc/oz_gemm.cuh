@@ -170,23 +170,31 @@ __device__ __forceinline__ void q_add_shifted(uint32_t (*q)[W], const uint32_t *
 // The reference's two 64-bit sums (OUT_PAIRS): bin j goes to the low word pair
 // q[0..1] with weight 2^(b t), t = J-1-j, when t < g0, else to q[2..3] with
 // weight 2^(b (t-g0)); both wrap modulo 2^64 like the reference's accumulators.
+// The word pair is a template argument: a runtime index into q would place the
+// whole accumulator array in local memory.
+template <int W, int NV, int BASE>
+__device__ __forceinline__ void pairs_add_at(uint32_t (*q)[W], const uint32_t *v, int sh) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        const int32_t iv = __float2int_rz(__uint_as_float(v[i]));
+        const uint32_t ext = static_cast<uint32_t>(iv >> 31);
+        if (sh < 32) {
+            const uint32_t lo = static_cast<uint32_t>(iv) << sh;
+            const uint32_t hi = __funnelshift_l(static_cast<uint32_t>(iv), ext, sh);
+            asm("add.cc.u32 %0, %0, %2;\n\taddc.u32 %1, %1, %3;" : "+r"(q[i][BASE]), "+r"(q[i][BASE + 1]) : "r"(lo), "r"(hi));
+        } else {
+            q[i][BASE + 1] += static_cast<uint32_t>(iv) << (sh - 32);
+        }
+    }
+}
+
 template <int W, int NV>
 __device__ __forceinline__ void pairs_add(uint32_t (*q)[W], const uint32_t *v, int t, int b, int g0) {
     if constexpr (W >= 4) {
-        const int base = t < g0 ? 0 : 2;
-        const int sh = b * (t < g0 ? t : t - g0);
-#pragma unroll
-        for (int i = 0; i < NV; ++i) {
-            const int32_t iv = __float2int_rz(__uint_as_float(v[i]));
-            const uint32_t ext = static_cast<uint32_t>(iv >> 31);
-            if (sh < 32) {
-                const uint32_t lo = static_cast<uint32_t>(iv) << sh;
-                const uint32_t hi = __funnelshift_l(static_cast<uint32_t>(iv), ext, sh);
-                asm("add.cc.u32 %0, %0, %2;\n\taddc.u32 %1, %1, %3;" : "+r"(q[i][base]), "+r"(q[i][base + 1]) : "r"(lo), "r"(hi));
-            } else {
-                q[i][base + 1] += static_cast<uint32_t>(iv) << (sh - 32);
-            }
-        }
+        if (t < g0)
+            pairs_add_at<W, NV, 0>(q, v, b * t);
+        else
+            pairs_add_at<W, NV, 2>(q, v, b * (t - g0));
     }
 }
 
@@ -360,7 +368,8 @@ template <int BN, int W, int KC>
 __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_constant__ GemmArgs g) {
     constexpr int PARTS = kEpiWarps / 4;          // drain warps sharing one TMEM lane quadrant
     constexpr int COLS = BN / PARTS;              // columns per drain thread
-    constexpr int DB = (COLS <= 24) ? COLS : 16;  // columns per TMEM load batch
+    // columns per TMEM load batch; narrower where the accumulators leave few registers
+    constexpr int DB = (COLS * (W + 1) > 72) ? 8 : ((COLS <= 24) ? COLS : 16);
     static_assert(COLS % 4 == 0 && COLS % DB == 0, "BN must split into 4-column parts");
 
     extern __shared__ uint8_t smem_raw[];
