@@ -238,6 +238,183 @@ def batched_run(n_probs, dev, stream, oz, O, torch):
             "speedup": p_ms / g_ms}
 
 
+def device_phi(shape, seed, phi, dev, torch):
+    """a_ij = (U(0,1) - 0.5) exp(phi N(0,1)) drawn on the device (torch's Philox
+    generator): the same family as the oracle's gen_phi, for operands too large
+    to draw on the host."""
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    x = torch.rand(shape, generator=g, dtype=torch.float64, device=dev).sub_(0.5)
+    x.mul_(torch.randn(shape, generator=g, dtype=torch.float64, device=dev).mul_(phi).exp_())
+    return x
+
+
+def sampled_errors(dA, dB, dC, n, seed, O, torch):
+    """Errors of n sampled entries of dC against the exact products (and MPFR-106
+    when libmpfr loads): only the sampled rows of A and columns of B leave the GPU."""
+    M, N = dC.shape
+    r, c = O.sample_indices(M, N, n, seed)
+    ri = torch.from_numpy(r.astype(np.int64)).to(dA.device)
+    ci = torch.from_numpy(c.astype(np.int64)).to(dA.device)
+    As = dA.index_select(0, ri).cpu().numpy()
+    Bs = dB.index_select(1, ci).cpu().numpy()
+    got = dC[ri, ci].cpu().numpy()
+    idx = np.arange(n, dtype=np.int32)
+    ex, _ = O.exact_entries(As, Bs, idx, idx)
+    out = {"normwise_rel_vs_exact": float(np.linalg.norm(got - ex) / max(np.linalg.norm(ex), 1e-300)),
+           "max_rel_vs_exact": float(np.max(np.abs(got - ex) / np.maximum(np.abs(ex), 1e-300))),
+           "entries": n}
+    mp = O.mpfr_entries(As, Bs, idx, idx)
+    if mp is not None:
+        out["normwise_rel_vs_mpfr106"] = float(np.linalg.norm(got - mp) / max(np.linalg.norm(mp), 1e-300))
+    return out
+
+
+def time_device(fn, torch, stream, reps=1):
+    """Mean device time (ms) of fn() over reps calls, CUDA events on the stream."""
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def long_k_run(dev, stream, oz, O, torch):
+    """The long-K workload: M = N = 8192, K = 65536, phi = 1, and the
+    ill-conditioned variant with row i of A scaled by 2^(-40 i / M); the accurate
+    mode (s = 8, full pair set) and the precision knob at 1e-15, against cuBLAS
+    FP64 on the same operands."""
+    Ml, Nl, Kl = 8192, 8192, 65536
+    flops = 2.0 * Ml * Nl * Kl
+    dB = device_phi((Kl, Nl), 32, 1.0, dev, torch)
+    dC = torch.empty((Ml, Nl), dtype=torch.float64, device=dev)
+    out = {"workload": "M = N = 8192, K = 65536, phi = 1 (device-drawn operands)", "effective_flop": flops}
+    for name in ("phi1", "ill_conditioned"):
+        dA = device_phi((Ml, Kl), 31, 1.0, dev, torch)
+        if name == "ill_conditioned":
+            dA.mul_(torch.exp2(-40.0 * torch.arange(Ml, dtype=torch.float64, device=dev) / Ml)[:, None])
+        res = {}
+        for label in ("accurate_s8_full", "adaptive_1e-15"):
+            h = oz.Handle()
+            if label == "accurate_s8_full":  # the accurate mode's configuration
+                h.set_slices(8)
+                h.set_bins(15)
+            else:
+                h.set_error_bound(BOUND)
+
+            def call():
+                if h.dgemm_device(Ml, Nl, Kl, dA.data_ptr(), Kl, dB.data_ptr(), Nl, dC.data_ptr(), Nl,
+                                  stream.cuda_stream):
+                    raise RuntimeError(h.last_error())
+
+            call()
+            ms = time_device(call, torch, stream, 2)
+            if h.sync():
+                raise RuntimeError(h.last_error())
+            cfg = h.config()
+            res[label] = {"value": flops / (ms * 1e-3) / 1e12, "unit": UNIT, "ms": ms, "slices": cfg["slices"],
+                          "bins": cfg["bins"], "accuracy": sampled_errors(dA, dB, dC, 256, 5, O, torch)}
+            h.close()
+        if name == "phi1":
+            ms = time_device(lambda: torch.matmul(dA, dB, out=dC), torch, stream, 1)
+            res["cublas_dgemm"] = {"value": flops / (ms * 1e-3) / 1e12, "unit": UNIT, "ms": ms,
+                                   "accuracy": sampled_errors(dA, dB, dC, 256, 5, O, torch)}
+        out[name] = res
+        del dA
+    return out
+
+
+def mix_sizes(n=64, seed=5, lo=1024, hi=16384):
+    """The accuracy-adaptive mix: n square sizes log-uniform in [lo, hi] plus one
+    hi^3, each with phi from {0.5, 1, 2, 4} and a bound from {1e-8, 1e-11, 1e-13,
+    1e-15}."""
+    g = np.random.default_rng(seed)
+    sz = [int(x) for x in np.exp(g.uniform(np.log(lo), np.log(hi), n))] + [hi]
+    phis = g.choice([0.5, 1.0, 2.0, 4.0], n + 1)
+    bounds = g.choice([1e-8, 1e-11, 1e-13, 1e-15], n + 1)
+    return list(zip(sz, phis.tolist(), bounds.tolist()))
+
+
+def mix_run(n, dev, stream, oz, O, torch):
+    """Per-problem calls over the mix: the precision knob (each problem's own
+    bound) against the plain accurate configuration (s = 8, full pair set) and
+    cuBLAS FP64, one problem resident at a time.  Errors are normwise over the
+    whole of C against a 16-slice Ozaki product (itself checked on sampled
+    entries against the exact products): with heavy-tailed entries (phi = 4) a
+    few large entries carry the norm of C, so a sampled normwise error says
+    little about the whole matrix."""
+    probs = mix_sizes(n)
+
+    def handle(slices=0, bins=0, bound=0.0):
+        h = oz.Handle()
+        if slices:
+            h.set_slices(slices)
+            h.set_bins(bins)
+        if bound:
+            h.set_error_bound(bound)
+        return h
+
+    ha, hp, hr = handle(), handle(8, 15), handle(16, 16)  # knob; accurate mode's configuration; reference
+    tot = {"adaptive": 0.0, "plain_s8_full": 0.0, "cublas_dgemm": 0.0}
+    flops_all, met, worst_ratio, ref_worst, hist, per = 0.0, 0, 0.0, 0.0, {}, []
+    for i, (m, phi, bound) in enumerate(probs):
+        dA = device_phi((m, m), 100 + i, phi, dev, torch)
+        dB = device_phi((m, m), 200 + i, phi, dev, torch)
+        dR = torch.empty((m, m), dtype=torch.float64, device=dev)
+        dC = torch.empty_like(dR)
+        flops = 2.0 * m ** 3
+        flops_all += flops
+        ha.set_error_bound(bound)
+
+        def call(h, out):
+            if h.dgemm_device(m, m, m, dA.data_ptr(), m, dB.data_ptr(), m, out.data_ptr(), m, stream.cuda_stream):
+                raise RuntimeError(h.last_error())
+
+        call(hr, dR)
+        ref_worst = max(ref_worst, sampled_errors(dA, dB, dR, 64, i, O, torch)["normwise_rel_vs_exact"])
+        rn = torch.linalg.norm(dR).item()
+        call(hp, dC)
+        tp = time_device(lambda: call(hp, dC), torch, stream)
+        ep = torch.linalg.norm(dC - dR).item() / rn
+        call(ha, dC)
+        ta = time_device(lambda: call(ha, dC), torch, stream)
+        for h in (ha, hp, hr):
+            if h.sync():
+                raise RuntimeError(h.last_error())
+        s = ha.config()["slices"]
+        ea = torch.linalg.norm(dC - dR).item() / rn
+        tc = time_device(lambda: torch.matmul(dA, dB, out=dC), torch, stream)
+        ec = torch.linalg.norm(dC - dR).item() / rn
+        tot["adaptive"] += ta
+        tot["plain_s8_full"] += tp
+        tot["cublas_dgemm"] += tc
+        met += int(ea <= bound)
+        worst_ratio = max(worst_ratio, ea / bound)
+        hist[str(s)] = hist.get(str(s), 0) + 1
+        per.append([m, phi, bound, s, round(ta, 3), round(tp, 3), round(tc, 3), ea, ep, ec])
+        del dA, dB, dR, dC
+    for h in (ha, hp, hr):
+        h.close()
+    return {"workload": "%d square DGEMMs, size log-uniform in [1024, 16384] (seed 5), plus one 16384^3; "
+                        "phi from {0.5, 1, 2, 4}, bound from {1e-8, 1e-11, 1e-13, 1e-15} per problem; "
+                        "device-drawn operands" % n,
+            "effective_flop": flops_all,
+            "error_reference": {"what": "Ozaki, 16 slices, triangular pair set, normwise over all of C",
+                                "its_worst_sampled_normwise_vs_exact": ref_worst},
+            "adaptive": {"value": flops_all / (tot["adaptive"] * 1e-3) / 1e12, "unit": UNIT, "ms": tot["adaptive"],
+                         "slices_hist": hist, "bounds_met": met, "problems": len(probs),
+                         "worst_err_over_bound": worst_ratio},
+            "plain_s8_full": {"value": flops_all / (tot["plain_s8_full"] * 1e-3) / 1e12, "unit": UNIT,
+                              "ms": tot["plain_s8_full"]},
+            "cublas_dgemm": {"value": flops_all / (tot["cublas_dgemm"] * 1e-3) / 1e12, "unit": UNIT,
+                             "ms": tot["cublas_dgemm"]},
+            "per_problem": {"columns": ["n", "phi", "bound", "slices", "adaptive_ms", "plain_ms", "cublas_ms",
+                                        "adaptive_err", "plain_err", "cublas_err"], "rows": per}}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -281,6 +458,8 @@ def main():
     ap.add_argument("--slices", type=int, default=0, help="fixed triangular slice count for --profile-only")
     ap.add_argument("--batched", type=int, default=512, help="problems in the batched comparison (0: skip)")
     ap.add_argument("--no-autotune", action="store_true", help="use the planner's cost-model plans")
+    ap.add_argument("--longk", action="store_true", help="add the long-K workload (8192^2 x 65536, ~1 min)")
+    ap.add_argument("--mix", type=int, default=0, help="add the accuracy-adaptive mix of this many problems")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -430,6 +609,8 @@ def main():
     err_cublas = O.error_report(dC.cpu().numpy(), A, B, r, c, exact, absdot)
 
     batched = batched_run(args.batched, dev, stream, oz, O, torch) if args.batched > 0 and rank == 0 else None
+    long_k = long_k_run(dev, stream, oz, O, torch) if args.longk and rank == 0 else None
+    mix = mix_run(args.mix, dev, stream, oz, O, torch) if args.mix > 0 and rank == 0 else None
 
     peaks = load_peaks()
     mma_flops = 2.0 * cfg["pairs"] * M * N * K
@@ -461,6 +642,8 @@ def main():
                          "algorithmic": "2 * pairs * M * N * K bf16 MMA flops per launch"},
             "gpu_launches": gpu_launches,
             "batched": batched,
+            "long_k": long_k,
+            "adaptive_mix": mix,
             "autotuned": {s: {k: v for k, v in c.items() if k in ("tile_n", "k_chunk", "stages", "blocks", "block_lo",
                                                                  "block_nb")} for s, c in tuned.items()}
             if tuned else None,
