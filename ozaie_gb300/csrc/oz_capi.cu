@@ -303,6 +303,8 @@ void gemm_args_from_plan(GemmArgs *g, const Plan &p, int out_mode, int *err, uns
     g->timeout_ns = timeout_ns;
     g->alpha = 1.0;
     g->beta = 0.0;
+    g->n_acc = p.n_acc;
+    for (int a = 0; a < kMaxAcc; ++a) g->acc_t0[a] = p.acc_t0[a];
     g->G = p.G;
     for (int i = 0; i < p.G; ++i) {
         g->blk_lo[i] = p.blk_lo[i];
@@ -343,7 +345,13 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
     g.total_tiles = p.tiles_m * p.tiles_n;
     g.alpha = o.alpha;
     g.beta = o.beta;
-    if (out_mode == OUT_PAIRS) g.pair_g0 = reference_first_group(o.K, p.cfg.b, p.cfg.s);
+    if (out_mode == OUT_PAIRS) {
+        // the reference's two sums: bins t < g0 and t >= g0, each modulo 2^64
+        g.pair_g0 = reference_first_group(o.K, p.cfg.b, p.cfg.s);
+        g.n_acc = g.pair_g0 < p.cfg.J ? 2 : 1;
+        g.acc_t0[0] = 0;
+        g.acc_t0[1] = g.pair_g0;
+    }
 #ifdef OZGB_PROBE
     // probe builds: per-CTA cycle counters of the GEMM roles, summarised on stderr
     static unsigned long long *probe = nullptr;

@@ -30,8 +30,12 @@
 //     chunk (after waiting for their drain): a drain overlaps the UMMAs of the
 //     other blocks.  The first UMMA of a block after a drain overwrites the
 //     accumulators (enable_input_d = 0), so TMEM is never cleared explicitly.
-//   * Drain (warps 2..17): TMEM -> registers, fp32 -> int32 (exact), shifted by
-//     b(J-1-j) and added into a W-word two's complement accumulator per element.
+//   * Drain (warps 2..17): TMEM -> registers, fp32 -> int32 (exact), then one
+//     32 x 32 -> 64-bit multiply-add by 2^rel into the 64-bit accumulator of the
+//     bin's group (consecutive bins whose weights relative to the group's first
+//     bin stay <= 2^30).  The W-word exact sum is assembled once per element in
+//     the epilogue.  Integer ALU work competes with the single MMA-issuing
+//     thread, so the drain keeps it to two instructions per value.
 //   * Epilogue: the exact accumulator q is rounded once to FP64 with the scale
 //     2^{Er+Ec-2044-b(J+1)} (round-to-nearest, or the reference's truncating
 //     decode, or written raw for parity dumps).
@@ -45,157 +49,79 @@
 
 namespace ozgb {
 
-// ------------------------------------------------------------------ q adds
-// q += lo * 2^(32*K0) + hi * 2^(32*(K0+1)) + ext * (2^(32*(K0+2)) + ...), one carry chain.
-template <int W, int K0>
-struct QAdd;
-
-template <>
-struct QAdd<2, 0> {
-    __device__ __forceinline__ static void run(uint32_t *q, uint32_t lo, uint32_t hi, uint32_t) {
-        asm("add.cc.u32 %0, %0, %2;\n\taddc.u32 %1, %1, %3;" : "+r"(q[0]), "+r"(q[1]) : "r"(lo), "r"(hi));
-    }
-};
-template <>
-struct QAdd<2, 1> {
-    __device__ __forceinline__ static void run(uint32_t *q, uint32_t lo, uint32_t, uint32_t) { q[1] += lo; }
-};
-template <>
-struct QAdd<3, 0> {
-    __device__ __forceinline__ static void run(uint32_t *q, uint32_t lo, uint32_t hi, uint32_t ext) {
-        asm("add.cc.u32 %0, %0, %3;\n\taddc.cc.u32 %1, %1, %4;\n\taddc.u32 %2, %2, %5;"
-            : "+r"(q[0]), "+r"(q[1]), "+r"(q[2])
-            : "r"(lo), "r"(hi), "r"(ext));
-    }
-};
-template <>
-struct QAdd<3, 1> {
-    __device__ __forceinline__ static void run(uint32_t *q, uint32_t lo, uint32_t hi, uint32_t) {
-        asm("add.cc.u32 %0, %0, %2;\n\taddc.u32 %1, %1, %3;" : "+r"(q[1]), "+r"(q[2]) : "r"(lo), "r"(hi));
-    }
-};
-template <>
-struct QAdd<3, 2> {
-    __device__ __forceinline__ static void run(uint32_t *q, uint32_t lo, uint32_t, uint32_t) { q[2] += lo; }
-};
-template <>
-struct QAdd<4, 0> {
-    __device__ __forceinline__ static void run(uint32_t *q, uint32_t lo, uint32_t hi, uint32_t ext) {
-        asm("add.cc.u32 %0, %0, %4;\n\taddc.cc.u32 %1, %1, %5;\n\taddc.cc.u32 %2, %2, %6;\n\taddc.u32 %3, %3, %6;"
-            : "+r"(q[0]), "+r"(q[1]), "+r"(q[2]), "+r"(q[3])
-            : "r"(lo), "r"(hi), "r"(ext));
-    }
-};
-template <>
-struct QAdd<4, 1> {
-    __device__ __forceinline__ static void run(uint32_t *q, uint32_t lo, uint32_t hi, uint32_t ext) {
-        asm("add.cc.u32 %0, %0, %3;\n\taddc.cc.u32 %1, %1, %4;\n\taddc.u32 %2, %2, %5;"
-            : "+r"(q[1]), "+r"(q[2]), "+r"(q[3])
-            : "r"(lo), "r"(hi), "r"(ext));
-    }
-};
-template <>
-struct QAdd<4, 2> {
-    __device__ __forceinline__ static void run(uint32_t *q, uint32_t lo, uint32_t hi, uint32_t) {
-        asm("add.cc.u32 %0, %0, %2;\n\taddc.u32 %1, %1, %3;" : "+r"(q[2]), "+r"(q[3]) : "r"(lo), "r"(hi));
-    }
-};
-template <>
-struct QAdd<4, 3> {
-    __device__ __forceinline__ static void run(uint32_t *q, uint32_t lo, uint32_t, uint32_t) { q[3] += lo; }
-};
-template <>
-struct QAdd<5, 0> {
-    __device__ __forceinline__ static void run(uint32_t *q, uint32_t lo, uint32_t hi, uint32_t ext) {
-        asm("add.cc.u32 %0, %0, %5;\n\taddc.cc.u32 %1, %1, %6;\n\taddc.cc.u32 %2, %2, %7;\n\t"
-            "addc.cc.u32 %3, %3, %7;\n\taddc.u32 %4, %4, %7;"
-            : "+r"(q[0]), "+r"(q[1]), "+r"(q[2]), "+r"(q[3]), "+r"(q[4])
-            : "r"(lo), "r"(hi), "r"(ext));
-    }
-};
-template <>
-struct QAdd<5, 1> {
-    __device__ __forceinline__ static void run(uint32_t *q, uint32_t lo, uint32_t hi, uint32_t ext) {
-        asm("add.cc.u32 %0, %0, %4;\n\taddc.cc.u32 %1, %1, %5;\n\taddc.cc.u32 %2, %2, %6;\n\taddc.u32 %3, %3, %6;"
-            : "+r"(q[1]), "+r"(q[2]), "+r"(q[3]), "+r"(q[4])
-            : "r"(lo), "r"(hi), "r"(ext));
-    }
-};
-template <>
-struct QAdd<5, 2> {
-    __device__ __forceinline__ static void run(uint32_t *q, uint32_t lo, uint32_t hi, uint32_t ext) {
-        asm("add.cc.u32 %0, %0, %3;\n\taddc.cc.u32 %1, %1, %4;\n\taddc.u32 %2, %2, %5;"
-            : "+r"(q[2]), "+r"(q[3]), "+r"(q[4])
-            : "r"(lo), "r"(hi), "r"(ext));
-    }
-};
-template <>
-struct QAdd<5, 3> {
-    __device__ __forceinline__ static void run(uint32_t *q, uint32_t lo, uint32_t hi, uint32_t) {
-        asm("add.cc.u32 %0, %0, %2;\n\taddc.u32 %1, %1, %3;" : "+r"(q[3]), "+r"(q[4]) : "r"(lo), "r"(hi));
-    }
-};
-template <>
-struct QAdd<5, 4> {
-    __device__ __forceinline__ static void run(uint32_t *q, uint32_t lo, uint32_t, uint32_t) { q[4] += lo; }
-};
-
-// Adds the n values v[] (fp32 holding exact integers) shifted left by 32*K0 + r
-// into the accumulators q[0..n).
-template <int W, int K0, int NV>
-__device__ __forceinline__ void q_add_block(uint32_t (*q)[W], const uint32_t *v, int r) {
-#pragma unroll
-    for (int i = 0; i < NV; ++i) {
-        const int32_t iv = __float2int_rz(__uint_as_float(v[i]));
-        const uint32_t ext = static_cast<uint32_t>(iv >> 31);
-        const uint32_t lo = static_cast<uint32_t>(iv) << r;
-        const uint32_t hi = __funnelshift_l(static_cast<uint32_t>(iv), ext, r);
-        QAdd<W, K0>::run(q[i], lo, hi, ext);
-    }
+// ------------------------------------------------------------ drain adds
+// d = a * m + c with a 64-bit result: one multiply-add per drained value.
+__device__ __forceinline__ long long mad_wide(int32_t a, int32_t m, long long c) {
+    long long d;
+    asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(m), "l"(c));
+    return d;
 }
 
-template <int W, int NV>
-__device__ __forceinline__ void q_add_shifted(uint32_t (*q)[W], const uint32_t *v, int sh) {
-    const int k = sh >> 5, r = sh & 31;
-    switch (k) {
-        case 0: q_add_block<W, 0, NV>(q, v, r); break;
-        case 1: if constexpr (W > 1) q_add_block<W, 1, NV>(q, v, r); break;
-        case 2: if constexpr (W > 2) q_add_block<W, 2, NV>(q, v, r); break;
-        case 3: if constexpr (W > 3) q_add_block<W, 3, NV>(q, v, r); break;
-        case 4: if constexpr (W > 4) q_add_block<W, 4, NV>(q, v, r); break;
-        default: break;
-    }
-}
-
-// The reference's two 64-bit sums (OUT_PAIRS): bin j goes to the low word pair
-// q[0..1] with weight 2^(b t), t = J-1-j, when t < g0, else to q[2..3] with
-// weight 2^(b (t-g0)); both wrap modulo 2^64 like the reference's accumulators.
-// The word pair is a template argument: a runtime index into q would place the
-// whole accumulator array in local memory.
-template <int W, int NV, int BASE>
-__device__ __forceinline__ void pairs_add_at(uint32_t (*q)[W], const uint32_t *v, int sh) {
+// acc[i][A] += v[i] * 2^rel modulo 2^64 for NV fp32 values holding exact
+// integers (|v| <= 2^24).  Exact-mode plans keep rel <= 30; the paired output
+// of the reference (sums modulo 2^64) may need up to 63.
+template <int NA, int A, int NV>
+__device__ __forceinline__ void acc_add(long long (*acc)[NA], const uint32_t *v, int rel) {
+    if (rel <= 30) {
+        const int32_t m = 1 << rel;
 #pragma unroll
-    for (int i = 0; i < NV; ++i) {
-        const int32_t iv = __float2int_rz(__uint_as_float(v[i]));
-        const uint32_t ext = static_cast<uint32_t>(iv >> 31);
-        if (sh < 32) {
-            const uint32_t lo = static_cast<uint32_t>(iv) << sh;
-            const uint32_t hi = __funnelshift_l(static_cast<uint32_t>(iv), ext, sh);
-            asm("add.cc.u32 %0, %0, %2;\n\taddc.u32 %1, %1, %3;" : "+r"(q[i][BASE]), "+r"(q[i][BASE + 1]) : "r"(lo), "r"(hi));
-        } else {
-            q[i][BASE + 1] += static_cast<uint32_t>(iv) << (sh - 32);
+        for (int i = 0; i < NV; ++i) acc[i][A] = mad_wide(__float2int_rz(__uint_as_float(v[i])), m, acc[i][A]);
+    } else if (rel <= 36) {
+        const int k = rel - 30;  // |v| 2^k < 2^31
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            const uint32_t iv = static_cast<uint32_t>(__float2int_rz(__uint_as_float(v[i])));
+            acc[i][A] = mad_wide(static_cast<int32_t>(iv << k), 1 << 30, acc[i][A]);
+        }
+    } else if (rel < 64) {
+        const int k = rel - 32;  // only the high word changes (modulo 2^64)
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            const uint32_t iv = static_cast<uint32_t>(__float2int_rz(__uint_as_float(v[i])));
+            acc[i][A] += static_cast<long long>(static_cast<unsigned long long>(iv << k) << 32);
         }
     }
 }
 
-template <int W, int NV>
-__device__ __forceinline__ void pairs_add(uint32_t (*q)[W], const uint32_t *v, int t, int b, int g0) {
-    if constexpr (W >= 4) {
-        if (t < g0)
-            pairs_add_at<W, NV, 0>(q, v, b * t);
-        else
-            pairs_add_at<W, NV, 2>(q, v, b * (t - g0));
+// The accumulator index is a template argument: a runtime index into acc would
+// place the whole array in local memory.
+template <int NA, int NV>
+__device__ __forceinline__ void acc_add_group(long long (*acc)[NA], const uint32_t *v, int a, int rel) {
+    switch (a) {
+        case 0: acc_add<NA, 0, NV>(acc, v, rel); break;
+        case 1: if constexpr (NA > 1) acc_add<NA, 1, NV>(acc, v, rel); break;
+        case 2: if constexpr (NA > 2) acc_add<NA, 2, NV>(acc, v, rel); break;
+        case 3: if constexpr (NA > 3) acc_add<NA, 3, NV>(acc, v, rel); break;
+        default: break;
     }
+}
+
+// q += x * 2^sh for a signed 64-bit x, q two's complement in W words (epilogue).
+template <int W>
+__device__ __forceinline__ void q_add_i64(uint32_t (&q)[W], long long x, int sh) {
+    const int k = sh >> 5, r = sh & 31;
+    const uint32_t lo = static_cast<uint32_t>(x);
+    const uint32_t hi = static_cast<uint32_t>(static_cast<unsigned long long>(x) >> 32);
+    const uint32_t ext = static_cast<uint32_t>(x >> 63);
+    const uint32_t p0 = lo << r, p1 = __funnelshift_l(lo, hi, r), p2 = __funnelshift_l(hi, ext, r);
+    uint32_t carry = 0;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        const int d = w - k;
+        const uint32_t a = d < 0 ? 0u : d == 0 ? p0 : d == 1 ? p1 : d == 2 ? p2 : ext;
+        const unsigned long long sum = static_cast<unsigned long long>(q[w]) + a + carry;
+        q[w] = static_cast<uint32_t>(sum);
+        carry = static_cast<uint32_t>(sum >> 32);
+    }
+}
+
+// TMEM columns per load batch of a drain thread: the widest that divides its
+// columns and leaves the accumulators (2 NA registers per column) room.
+__host__ __device__ constexpr int drain_batch(int cols, int acc_regs) {
+    return (cols % 16 == 0 && acc_regs + 16 <= 64)   ? 16
+           : (cols % 12 == 0 && acc_regs + 12 <= 64) ? 12
+           : (cols % 8 == 0 && acc_regs + 8 <= 64)   ? 8
+                                                     : 4;
 }
 
 // ------------------------------------------------------------ q -> double
@@ -368,8 +294,9 @@ template <int BN, int W, int KC>
 __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_constant__ GemmArgs g) {
     constexpr int PARTS = kEpiWarps / 4;          // drain warps sharing one TMEM lane quadrant
     constexpr int COLS = BN / PARTS;              // columns per drain thread
-    // columns per TMEM load batch; narrower where the accumulators leave few registers
-    constexpr int DB = (COLS * (W + 1) > 72) ? 8 : ((COLS <= 24) ? COLS : 16);
+    constexpr int NA = W > 2 ? W - 1 : 1;         // 64-bit accumulator groups per column
+    constexpr int DB = drain_batch(COLS, 2 * NA * COLS);
+    static_assert(NA <= kMaxAcc, "accumulator groups");
     static_assert(COLS % 4 == 0 && COLS % DB == 0, "BN must split into 4-column parts");
 
     extern __shared__ uint8_t smem_raw[];
@@ -602,7 +529,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
         const int part = ew >> 2;  // which COLS-wide column slice of the tile
         const uint32_t trow = tmem + (static_cast<uint32_t>(32 * qd) << 16) + static_cast<uint32_t>(part * COLS);
 
-        uint32_t q[COLS][W];
+        long long acc[COLS][NA];
         uint64_t fphase = 0;
         uint32_t prev = 0;
         bool ok = true;
@@ -612,7 +539,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
 #pragma unroll
             for (int i = 0; i < COLS; ++i)
 #pragma unroll
-                for (int w = 0; w < W; ++w) q[i][w] = 0;
+                for (int a = 0; a < NA; ++a) acc[i][a] = 0;
 
             DrainSchedule ds;
             ds.init(g);
@@ -644,7 +571,16 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                             }
                         const int hi = lo + nb - 1;
                         for (int j = lo; j <= hi; ++j) {
-                            const int sh = g.b * (g.J - 1 - j);
+                            // accumulator group of bin j and its weight within the group
+                            const int t = g.J - 1 - j;
+                            int a = 0, t0 = 0;
+#pragma unroll
+                            for (int x = 1; x < NA; ++x)
+                                if (x < g.n_acc && t >= g.acc_t0[x]) {
+                                    a = x;
+                                    t0 = g.acc_t0[x];
+                                }
+                            const int rel = g.b * (t - t0);
 #pragma unroll
                             for (int cb = 0; cb < COLS / DB; ++cb) {
                                 uint32_t v[DB];
@@ -652,10 +588,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                                 tmem_ld_wait();
 #pragma unroll
                                 for (int i = 0; i < DB; ++i) reg_fence(v[i]);
-                                if (g.out_mode == OUT_PAIRS)
-                                    pairs_add<W, DB>(q + cb * DB, v, g.J - 1 - j, g.b, g.pair_g0);
-                                else
-                                    q_add_shifted<W, DB>(q + cb * DB, v, sh);
+                                acc_add_group<NA, DB>(acc + cb * DB, v, a, rel);
                             }
                         }
                         // the block's accumulators are free for the next chunk (or tile)
@@ -676,23 +609,30 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
             if (row < tr.M) {
                 const int er = tr.er[row];
                 const int bJ1 = g.b * (g.J + 1);
+                // the exact sum of column i: sum_a acc[i][a] 2^(b acc_t0[a]) in W words
+                auto exact_q = [&](int i, uint32_t (&q)[W]) {
+#pragma unroll
+                    for (int w = 0; w < W; ++w) q[w] = 0;
+#pragma unroll
+                    for (int x = 0; x < NA; ++x)
+                        if (x < g.n_acc) q_add_i64<W>(q, acc[i][x], g.b * g.acc_t0[x]);
+                };
                 if (g.out_mode == OUT_PAIRS) {
                     // the reference's device output: lo, then hi with bits 51..62 = Er + Ec
-                    if constexpr (W >= 4) {
 #pragma unroll
-                        for (int i = 0; i < COLS; ++i) {
-                            const int col = col0 + i;
-                            if (col < tr.N) {
-                                long long *dst =
-                                    reinterpret_cast<long long *>(g.raw) + (static_cast<size_t>(row) * tr.N + col) * 2;
-                                const unsigned long long lo = (static_cast<unsigned long long>(q[i][1]) << 32) | q[i][0];
-                                unsigned long long hi = (static_cast<unsigned long long>(q[i][3]) << 32) | q[i][2];
-                                const unsigned long long scale =
-                                    static_cast<unsigned long long>(static_cast<uint32_t>(er + tr.ec[col]));
-                                hi = (hi & 0x8007FFFFFFFFFFFFull) | ((scale & 0xFFFull) << 51);
-                                dst[0] = static_cast<long long>(lo);
-                                dst[1] = static_cast<long long>(hi);
-                            }
+                    for (int i = 0; i < COLS; ++i) {
+                        const int col = col0 + i;
+                        if (col < tr.N) {
+                            long long *dst =
+                                reinterpret_cast<long long *>(g.raw) + (static_cast<size_t>(row) * tr.N + col) * 2;
+                            const unsigned long long lo = static_cast<unsigned long long>(acc[i][0]);
+                            unsigned long long hi = 0;
+                            if constexpr (NA > 1) hi = g.n_acc > 1 ? static_cast<unsigned long long>(acc[i][1]) : 0ull;
+                            const unsigned long long scale =
+                                static_cast<unsigned long long>(static_cast<uint32_t>(er + tr.ec[col]));
+                            hi = (hi & 0x8007FFFFFFFFFFFFull) | ((scale & 0xFFFull) << 51);
+                            dst[0] = static_cast<long long>(lo);
+                            dst[1] = static_cast<long long>(hi);
                         }
                     }
                 } else if (g.out_mode == OUT_RAW) {
@@ -700,10 +640,12 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                     for (int i = 0; i < COLS; ++i) {
                         const int col = col0 + i;
                         if (col < tr.N) {
+                            uint32_t q[W];
+                            exact_q(i, q);
                             int32_t *dst = g.raw + (static_cast<size_t>(row) * tr.N + col) * 4;
-                            const uint32_t ext = static_cast<uint32_t>(static_cast<int32_t>(q[i][W - 1]) >> 31);
+                            const uint32_t ext = static_cast<uint32_t>(static_cast<int32_t>(q[W - 1]) >> 31);
 #pragma unroll
-                            for (int w = 0; w < 4; ++w) dst[w] = static_cast<int32_t>(w < W ? q[i][w] : ext);
+                            for (int w = 0; w < 4; ++w) dst[w] = static_cast<int32_t>(w < W ? q[w] : ext);
                         }
                     }
                 } else {
@@ -713,7 +655,9 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                     for (int i = 0; i < COLS; ++i) {
                         const int col = col0 + i;
                         if (col < tr.N) {
-                            double v = q_to_double<W>(q[i], er + tr.ec[col], bJ1, g.out_mode);
+                            uint32_t q[W];
+                            exact_q(i, q);
+                            double v = q_to_double<W>(q, er + tr.ec[col], bJ1, g.out_mode);
                             // BLAS semantics: C is not read when beta == 0
                             if (!plain) v = g.beta == 0.0 ? g.alpha * v : fma(g.beta, crow[col], g.alpha * v);
                             crow[col] = v;

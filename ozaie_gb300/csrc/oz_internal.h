@@ -23,6 +23,7 @@ namespace ozgb {
 constexpr int BM = 128;         // rows of A per tile (UMMA M)
 constexpr int kMaxBins = 64;      // J limit
 constexpr int kMaxGroups = 8;     // drain groups limit
+constexpr int kMaxAcc = 4;        // 64-bit accumulator groups per element (drain)
 constexpr int kEpiWarps = 16;     // drain + epilogue warps: 4 per TMEM lane quadrant
 constexpr int kThreads = 64 + 32 * kEpiWarps;  // warp 0 producer, warp 1 MMA issuer, then the drain warps
 constexpr int kMaxAccWords = 5;
@@ -73,6 +74,13 @@ struct GemmArgs {
     int blk_period[kMaxGroups], blk_off[kMaxGroups];
     int total_tiles;  // tiles_m * tiles_n
     int pair_g0;      // OUT_PAIRS: bins in the low word group (the reference's first group)
+    // Accumulator groups of the drain: with t = J - 1 - j, bin j is added into the
+    // 64-bit accumulator a of its group (the last a with acc_t0[a] <= t) with
+    // weight 2^(b (t - acc_t0[a])); the exact sum is sum_a acc_a 2^(b acc_t0[a]).
+    // The planner keeps every weight <= 2^30 and every group's worst-case sum
+    // below 2^63.  OUT_PAIRS: groups {0, pair_g0}, each modulo 2^64.
+    int n_acc;
+    int acc_t0[kMaxAcc];
     double alpha, beta;  // C = alpha * (A B) + beta * C for OUT_RN / OUT_RZ_REF (1, 0: plain store)
 };
 

@@ -146,6 +146,8 @@ extern "C" ozgb_status ozgb_dgemm_device_noalloc(int M, int N, int K, const doub
     g.tmem_cols = p.tmem_cols;
     g.err = err;
     g.timeout_ns = 2000000000ull;
+    g.n_acc = p.n_acc;
+    for (int a = 0; a < kMaxAcc; ++a) g.acc_t0[a] = p.acc_t0[a];
     g.G = p.G;
     for (int i = 0; i < p.G; ++i) {
         g.blk_lo[i] = p.blk_lo[i];

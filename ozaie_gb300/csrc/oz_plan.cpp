@@ -187,11 +187,37 @@ bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std
         *err = "too many pairs per bin for exact fp32 accumulation of one 16-deep K step";
         return false;
     }
+    // Drain accumulator groups: consecutive t = J - 1 - j (increasing weight) share
+    // one 64-bit accumulator while the weight relative to the group's first bin
+    // stays <= 2^30 (one 32 x 32 -> 64-bit multiply-add per drained value) and the
+    // group's worst-case sum over all of K stays below 2^62.
+    int n_acc = 0, acc_t0[kMaxAcc] = {0};
+    {
+        long double gsum = 0.0L;
+        int t0 = 0;
+        for (int t = 0; t < J; ++t) {
+            const long double one = static_cast<long double>(pairs_in_bin(J - 1 - t, s)) * v2 * v2 * K;
+            const int rel = b * (t - t0);
+            const long double add = std::ldexp(one, rel);
+            if (n_acc > 0 && rel <= 30 && gsum + add < std::ldexp(1.0L, 62)) {
+                gsum += add;
+                continue;
+            }
+            if (n_acc == kMaxAcc) {
+                *err = "the exact accumulation needs more than " + std::to_string(kMaxAcc) + " 64-bit groups";
+                return false;
+            }
+            acc_t0[n_acc++] = t;
+            t0 = t;
+            gsum = one;
+        }
+    }
     const Variant *chosen = nullptr;
     for (const Variant &v : kVariants) {
         if (v.KC != 32) continue;
         if (hint.BN && v.BN != hint.BN) continue;
         if (v.W < hint.min_W) continue;
+        if (std::max(1, v.W - 1) < n_acc) continue;  // accumulator groups the variant holds
         if (v.BN * J > 512) continue;
         if (32 * v.W < bits) continue;
         chosen = &v;
@@ -204,6 +230,8 @@ bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std
     }
     p.BN = chosen->BN;
     p.W = chosen->W;
+    p.n_acc = n_acc;
+    for (int a = 0; a < kMaxAcc; ++a) p.acc_t0[a] = acc_t0[a];
 
     // ---- bin blocks: contiguous bin ranges of at most 256 columns; every UMMA of a
     // block spans the whole block (zero B slices pad the out-of-range q).  Measured

@@ -30,6 +30,7 @@ struct Plan {
     double model_cycles_per_kstep = 0;  // UMMA cost model of the chosen blocks
     int blk_lo[kMaxGroups] = {0}, blk_nb[kMaxGroups] = {0}, blk_p0[kMaxGroups] = {0}, blk_p1[kMaxGroups] = {0};
     int blk_period[kMaxGroups] = {0}, blk_off[kMaxGroups] = {0};
+    int n_acc = 0, acc_t0[kMaxAcc] = {0};  // drain accumulator groups (GemmArgs)
     GemmLaunchFn fn = nullptr;
 };
 
