@@ -645,7 +645,7 @@ def main():
             "long_k": long_k,
             "adaptive_mix": mix,
             "autotuned": {s: {k: v for k, v in c.items() if k in ("tile_n", "k_chunk", "stages", "blocks", "block_lo",
-                                                                 "block_nb")} for s, c in tuned.items()}
+                                                                 "block_nb", "issuers")} for s, c in tuned.items()}
             if tuned else None,
             "clocks": clk,
         }

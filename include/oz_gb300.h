@@ -73,6 +73,7 @@ typedef struct {
     int umma_per_kstep; /* UMMAs per 16-deep K step */
     int block_lo[8]; /* first bin of each block */
     int block_nb[8]; /* bins in each block */
+    int issuers;     /* threads issuing the UMMAs (bin blocks split between them) */
 } ozgb_config;
 
 /* ---------------------------------------------------------------- handles */

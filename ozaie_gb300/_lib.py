@@ -28,6 +28,7 @@ class OzgbConfig(ctypes.Structure):
         ("umma_per_kstep", ctypes.c_int),
         ("block_lo", ctypes.c_int * 8),
         ("block_nb", ctypes.c_int * 8),
+        ("issuers", ctypes.c_int),
     ]
 
     def as_dict(self):

@@ -304,6 +304,7 @@ void gemm_args_from_plan(GemmArgs *g, const Plan &p, int out_mode, int *err, uns
     g->alpha = 1.0;
     g->beta = 0.0;
     g->n_acc = p.n_acc;
+    g->n_iss = p.n_iss;
     for (int a = 0; a < kMaxAcc; ++a) g->acc_t0[a] = p.acc_t0[a];
     g->G = p.G;
     for (int i = 0; i < p.G; ++i) {
@@ -758,6 +759,7 @@ bool valid_mode(int mode) { return mode == OZGB_MODE_ACCURATE || mode == OZGB_MO
 void fill_blocks(const Plan &p, ozgb_config *out) {
     out->blocks = p.G;
     out->umma_per_kstep = p.mma_per_kstep;
+    out->issuers = p.n_iss;
     for (int i = 0; i < 8; ++i) {
         out->block_lo[i] = i < p.G ? p.blk_lo[i] : 0;
         out->block_nb[i] = i < p.G ? p.blk_nb[i] : 0;

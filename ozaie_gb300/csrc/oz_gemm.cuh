@@ -338,16 +338,17 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
+    const int n_iss = (g.G >= 2 && g.n_iss >= 2) ? 2 : 1;  // MMA-issuing threads (blocks split by parity)
     if (threadIdx.x == 0) {
         for (int i = 0; i < g.stages; ++i) {
             mbar_init(&full[i], 1);
-            mbar_init(&empty[i], 1);
+            mbar_init(&empty[i], n_iss);
         }
         for (int i = 0; i < g.G; ++i) {
             mbar_init(&gfull[i], 1);
             mbar_init(&gempty[i], kEpiWarps);
         }
-        mbar_init(mma_done, 1);
+        mbar_init(mma_done, n_iss);
         *abort_flag = (*reinterpret_cast<volatile int *>(g.err) != 0) ? 1 : 0;
         fence_mbar_init();
     }
@@ -414,9 +415,15 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
             for (long long c = (first > 0 ? first : 0); c < issued; ++c)
                 mbar_wait(&full[c % g.stages], static_cast<uint32_t>((c / g.stages) & 1), &zero, TO);
         }
-    } else if (warp == 1) {
-        // ---------------------------------------------------- MMA issuer
-        if (lane == 0) {
+    } else if (warp == 1 || warp == kIssuer2Warp) {
+        // ---------------------------------------------------- MMA issuers
+        // Issuer iss issues the UMMAs of the bin blocks blk with blk % n_iss == iss
+        // and commits every stage it has read to the stage's empty barrier.
+        const int iss = warp == 1 ? 0 : 1;
+        if (lane == 0 && iss < n_iss) {
+            uint32_t mine = 0;
+            for (int i = 0; i < g.G; ++i)
+                if (i % n_iss == iss) mine |= 1u << i;
             constexpr uint32_t a_step = (BM * KC * 2) >> 4;  // descriptor units (16 B)
             constexpr uint32_t b_step = (BN * KC * 2) >> 4;
             constexpr uint32_t sbo = KC * 16;
@@ -430,7 +437,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                 const uint32_t idesc_base = idesc_bf16_f32(BM, 16) & ~(0x3Fu << 17);
 #pragma unroll
                 for (int i = 0; i < kMaxGroups; ++i) {
-                    if (i < g.G) {
+                    if (i < g.G && ((mine >> i) & 1u)) {
                         blk_ad[i] = ad0 + static_cast<uint64_t>(g.blk_p0[i]) * a_step;
                         blk_bd[i] = bd0 + static_cast<uint64_t>(static_cast<int64_t>(g.blk_lo[i] - g.blk_p0[i]) * b_step);
                         blk_tm[i] = tmem + static_cast<uint32_t>(g.blk_lo[i] * BN);
@@ -439,7 +446,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                     }
                 }
             }
-            const uint32_t all = (1u << g.G) - 1u;
+            const uint32_t all = mine;
             uint64_t ephase = 0;            // per-block parity of gempty waits
             uint32_t prev = 0;              // blocks drained after the previous chunk (of any tile)
             uint32_t fresh = all;           // blocks whose next UMMA overwrites the accumulators
@@ -461,7 +468,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                 if (cur & kStageTerminate) break;
                 // issue order: blocks drained after this chunk, then the rest, then the
                 // blocks whose drain (after the previous chunk) must finish first
-                uint32_t order[3] = {cur & ~prev, all & ~cur & ~prev, prev};
+                uint32_t order[3] = {cur & all & ~prev, all & ~cur & ~prev, prev};
                 for (int cls = 0; ok && cls < 3; ++cls) {
                     uint32_t m = order[cls];
                     while (m) {
@@ -510,7 +517,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                     st = 0;
                     fparity ^= 1u;
                 }
-                prev = cur;
+                prev = cur & all;
             }
             if (!ok && !*vabort) {
                 atomicCAS(g.err, 0, DEVERR_TIMEOUT_MMA);

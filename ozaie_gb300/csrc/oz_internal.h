@@ -25,7 +25,11 @@ constexpr int kMaxBins = 64;      // J limit
 constexpr int kMaxGroups = 8;     // drain groups limit
 constexpr int kMaxAcc = 4;        // 64-bit accumulator groups per element (drain)
 constexpr int kEpiWarps = 16;     // drain + epilogue warps: 4 per TMEM lane quadrant
-constexpr int kThreads = 64 + 32 * kEpiWarps;  // warp 0 producer, warp 1 MMA issuer, then the drain warps
+// warp 0 producer, warp 1 MMA issuer, then the drain warps, then a second MMA
+// issuer (on another scheduler than the first: the bin blocks are split between
+// the two so neither issuing thread's instruction stream limits the tensor pipe)
+constexpr int kThreads = 64 + 32 * kEpiWarps + 32;
+constexpr int kIssuer2Warp = 2 + kEpiWarps;
 constexpr int kMaxAccWords = 5;
 
 // OUT_PAIRS writes the reference's device output (its C buffer before the host
@@ -81,6 +85,7 @@ struct GemmArgs {
     // below 2^63.  OUT_PAIRS: groups {0, pair_g0}, each modulo 2^64.
     int n_acc;
     int acc_t0[kMaxAcc];
+    int n_iss;  // MMA-issuing threads: 2 splits the bin blocks by index parity (G >= 2)
     double alpha, beta;  // C = alpha * (A B) + beta * C for OUT_RN / OUT_RZ_REF (1, 0: plain store)
 };
 

@@ -147,6 +147,7 @@ extern "C" ozgb_status ozgb_dgemm_device_noalloc(int M, int N, int K, const doub
     g.err = err;
     g.timeout_ns = 2000000000ull;
     g.n_acc = p.n_acc;
+    g.n_iss = p.n_iss;
     for (int a = 0; a < kMaxAcc; ++a) g.acc_t0[a] = p.acc_t0[a];
     g.G = p.G;
     for (int i = 0; i < p.G; ++i) {

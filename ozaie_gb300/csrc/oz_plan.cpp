@@ -380,6 +380,9 @@ bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std
         p.pad_hi = std::max(p.pad_hi, hi - p.blk_p0[g] - (s - 1));  // q = hi - p0 <= s - 1 + pad_hi
     }
 
+    // two issuing threads (bin blocks split by parity) unless the hint says one
+    p.n_iss = (p.G >= 2 && hint.issuers != 1) ? 2 : 1;
+
     // ---- pipeline: K chunk and stage count
     const size_t budget = kSmemLimit - kSmemReserve;
     const int kc_opts[2] = {32, 16};
@@ -461,7 +464,7 @@ std::vector<PlanHints> plan_candidates(int M, int N, int K, const OzConfig &cfg,
     std::vector<PlanHints> out;
     std::vector<Plan> plans;
     auto same = [](const Plan &x, const Plan &y) {
-        if (x.BN != y.BN || x.KC != y.KC || x.G != y.G || x.stages != y.stages) return false;
+        if (x.BN != y.BN || x.KC != y.KC || x.G != y.G || x.stages != y.stages || x.n_iss != y.n_iss) return false;
         for (int i = 0; i < x.G; ++i)
             if (x.blk_lo[i] != y.blk_lo[i] || x.blk_nb[i] != y.blk_nb[i]) return false;
         return true;
@@ -477,9 +480,20 @@ std::vector<PlanHints> plan_candidates(int M, int N, int K, const OzConfig &cfg,
         exact.KC = p.KC;
         exact.groups = p.G;
         exact.stages = p.stages;
+        exact.issuers = p.n_iss;
         for (int g = 0; g < kMaxGroups; ++g) exact.sizes[g] = g < p.G ? p.blk_nb[g] : 0;
         plans.push_back(p);
         out.push_back(exact);
+        if (p.n_iss == 2 && !h.issuers) {
+            // the same plan with one issuing thread
+            PlanHints one = exact;
+            one.issuers = 1;
+            Plan q;
+            if (make_plan(M, N, K, cfg, &q, &why, 0, 1 << 30, &one)) {
+                plans.push_back(q);
+                out.push_back(one);
+            }
+        }
     };
     try_add(PlanHints{});  // the cost-model choice
     const int bns[] = {128, 64, 48, 32, 16};

@@ -31,6 +31,7 @@ struct Plan {
     int blk_lo[kMaxGroups] = {0}, blk_nb[kMaxGroups] = {0}, blk_p0[kMaxGroups] = {0}, blk_p1[kMaxGroups] = {0};
     int blk_period[kMaxGroups] = {0}, blk_off[kMaxGroups] = {0};
     int n_acc = 0, acc_t0[kMaxAcc] = {0};  // drain accumulator groups (GemmArgs)
+    int n_iss = 1;                         // MMA-issuing threads
     GemmLaunchFn fn = nullptr;
 };
 
@@ -49,6 +50,7 @@ struct PlanHints {
     int BN = 0, KC = 0, groups = 0, stages = 0;
     int sizes[kMaxGroups] = {0};  // explicit bin-block sizes (groups of them), overriding the cost model
     int min_W = 0;                // at least this many accumulator words (4 for OUT_PAIRS)
+    int issuers = 0;              // MMA-issuing threads (1 or 2)
 };
 
 // Builds the plan for bins [bin_lo, bin_hi] of the pair set (the full set of
