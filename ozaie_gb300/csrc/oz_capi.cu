@@ -76,6 +76,8 @@ struct ozgb_context {
     cudaStream_t aux[kAux] = {};
     cudaEvent_t ev_fork = nullptr;
     cudaEvent_t ev_join[kAux] = {};
+    // host-array calls: the GEMM's first part done / its rows copied back (aux[0])
+    cudaEvent_t ev_part = nullptr, ev_part_copied = nullptr;
     // grouped calls under CUDA graphs (ozgb_set_graph): the two captured phases and
     // the inputs they were captured for; the knob statistics land in pinned memory
     std::vector<long long> gkey1, gkey2;
@@ -317,9 +319,43 @@ void gemm_args_from_plan(GemmArgs *g, const Plan &p, int out_mode, int *err, uns
     }
 }
 
+// Auxiliary streams and their events, created on first use.
+ozgb_status ensure_aux(ozgb_handle h) {
+    if (h->ev_fork) return OZGB_OK;
+    bool okc = cudaEventCreateWithFlags(&h->ev_part, cudaEventDisableTiming) == cudaSuccess &&
+               cudaEventCreateWithFlags(&h->ev_part_copied, cudaEventDisableTiming) == cudaSuccess;
+    for (int a = 0; okc && a < ozgb_context::kAux; ++a)
+        okc = cudaStreamCreateWithFlags(&h->aux[a], cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&h->ev_join[a], cudaEventDisableTiming) == cudaSuccess;
+    okc = okc && cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) == cudaSuccess;
+    if (!okc) return cuda_fail(h, cudaGetLastError(), "auxiliary streams");
+    return OZGB_OK;
+}
+
+int sm_count(int dev) {
+    static int cached[64] = {0};
+    if (dev < 0 || dev >= 64) return 148;
+    if (!cached[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 148;
+        cached[dev] = n;
+    }
+    return cached[dev];
+}
+
+// Host destination of C (the host-array entry point, C dense with N columns).
+// When C has more than one group of 8 row tiles, the GEMM runs as two launches:
+// the first covers full waves up to the end of the last group but one, and the
+// rows it completes are copied back on an auxiliary stream while the second
+// launch runs.  Splitting at a multiple of the grid keeps the number of waves.
+struct HostOut {
+    double *C;
+    bool copied;  // set when the split path has enqueued every copy of C
+};
+
 // Stages (b) and (c)+(d) for one problem whose exponents are in h->er / h->ec.
 ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, int out_mode, int32_t *raw,
-                               cudaStream_t st) {
+                               cudaStream_t st, HostOut *ho = nullptr) {
     if (!h->at.ensure(p.a_elems * 2) || !h->bt.ensure(p.b_elems * 2))
         return fail(h, OZGB_ERR_ALLOC, "slice buffers");
     uint16_t *at = static_cast<uint16_t *>(h->at.p), *bt = static_cast<uint16_t *>(h->bt.p);
@@ -366,9 +402,51 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
     cudaMemsetAsync(probe, 0, need * 8, st);
     g.probe = probe;
 #endif
-    p.fn(g, p.tiles_m * p.tiles_n, p.smem, st);
+    const int total = p.tiles_m * p.tiles_n;
+    int t_split = 0, rows_split = 0;
+    if (ho && (out_mode == OUT_RN || out_mode == OUT_RZ_REF) && o.ldc == o.N) {
+        const int grid = std::min(total, sm_count(h->device));
+        const int groups = (p.tiles_m + 7) / 8;  // grouped rasterisation: 8 row tiles per group
+        if (groups >= 2) {
+            const int before_last = (groups - 1) * 8 * p.tiles_n;
+            const int t1 = ((before_last + grid - 1) / grid) * grid;
+            if (t1 < total) {
+                t_split = t1;
+                rows_split = (groups - 1) * 8 * BM;
+            }
+        }
+    }
+    cudaError_t e;
+    if (t_split > 0) {
+        ozgb_status rc = ensure_aux(h);
+        if (rc) return rc;
+        g.total_tiles = t_split;
+        p.fn(g, t_split, p.smem, st);
+        cudaEventRecord(h->ev_part, st);
+        cudaStreamWaitEvent(h->aux[0], h->ev_part, 0);
+        const size_t n1 = static_cast<size_t>(rows_split) * o.N;
+        if ((e = cudaMemcpyAsync(ho->C, o.C, n1 * 8, cudaMemcpyDeviceToHost, h->aux[0])) != cudaSuccess)
+            return cuda_fail(h, e, "copy C (first rows)");
+        cudaEventRecord(h->ev_part_copied, h->aux[0]);
+        g.tile_begin = t_split;
+        g.total_tiles = total;
+        p.fn(g, total - t_split, p.smem, st);
+        h->launches += 2;
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(h, e, "slice-pair GEMM launch");
+        if (h->profiling) {
+            cudaEventRecord(h->ev[3], st);
+            h->ev_recorded = true;
+        }
+        const size_t n2 = static_cast<size_t>(o.M - rows_split) * o.N;
+        if ((e = cudaMemcpyAsync(ho->C + n1, o.C + n1, n2 * 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+            return cuda_fail(h, e, "copy C (last rows)");
+        cudaStreamWaitEvent(st, h->ev_part_copied, 0);
+        ho->copied = true;
+        return OZGB_OK;
+    }
+    p.fn(g, total, p.smem, st);
     h->launches += 1;
-    cudaError_t e = cudaGetLastError();
+    e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(h, e, "slice-pair GEMM launch");
 #ifdef OZGB_PROBE
     {
@@ -391,7 +469,7 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
 
 // The whole pipeline for one problem on device operands.
 ozgb_status enqueue_dgemm(ozgb_handle h, const Operands &o, int mode, cudaStream_t st, int out_mode_override = -1,
-                          int bin_lo = 0, int bin_hi = kMaxBins, int32_t *raw = nullptr) {
+                          int bin_lo = 0, int bin_hi = kMaxBins, int32_t *raw = nullptr, HostOut *ho = nullptr) {
     h->last_stream = st;
     if (h->profiling) cudaEventRecord(h->ev[0], st);
     const bool want_ss = h->err_bound > 0.0 && h->opt_slices <= 0;
@@ -415,8 +493,8 @@ ozgb_status enqueue_dgemm(ozgb_handle h, const Operands &o, int mode, cudaStream
     h->last = p;
     h->have_last = true;
     const int om = out_mode_override >= 0 ? out_mode_override : cfg.rounding;
-    if ((rc = enqueue_split_gemm(h, o, p, om, raw, st))) return rc;
-    if (h->profiling) {
+    if ((rc = enqueue_split_gemm(h, o, p, om, raw, st, ho))) return rc;
+    if (h->profiling && !(ho && ho->copied)) {
         cudaEventRecord(h->ev[3], st);
         h->ev_recorded = true;
     }
@@ -664,13 +742,7 @@ ozgb_status enqueue_grouped(ozgb_handle h, ozgb_problem *probs, int n, int mode,
     }
     if (!h->gslice.ensure(sl_total)) return fail(h, OZGB_ERR_ALLOC, "grouped slice buffer");
     uint8_t *gsl = static_cast<uint8_t *>(h->gslice.p);
-    if (!h->ev_fork) {
-        bool okc = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) == cudaSuccess;
-        for (int a = 0; okc && a < ozgb_context::kAux; ++a)
-            okc = cudaStreamCreateWithFlags(&h->aux[a], cudaStreamNonBlocking) == cudaSuccess &&
-                  cudaEventCreateWithFlags(&h->ev_join[a], cudaEventDisableTiming) == cudaSuccess;
-        if (!okc) return cuda_fail(h, cudaGetLastError(), "auxiliary streams");
-    }
+    if ((rc = ensure_aux(h))) return rc;
     std::vector<long long> key2 = key1;
     key2.insert(key2.end(), {reinterpret_cast<long long>(gsl), reinterpret_cast<long long>(h->err.p),
                              static_cast<long long>(h->timeout_ns)});
@@ -809,6 +881,8 @@ ozgb_status ozgb_destroy(ozgb_handle h) {
             if (h->ev_join[i]) cudaEventDestroy(h->ev_join[i]);
         }
         if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+        if (h->ev_part) cudaEventDestroy(h->ev_part);
+        if (h->ev_part_copied) cudaEventDestroy(h->ev_part_copied);
         if (h->knob_host) cudaFreeHost(h->knob_host);
     }
     delete h;
@@ -860,11 +934,12 @@ ozgb_status ozgb_dgemm(ozgb_handle h, int M, int N, int K, const double *A, cons
         return cuda_fail(h, e, "copy B");
     Operands o{M, N, K, static_cast<double *>(h->a.p), K, static_cast<double *>(h->b.p), N,
                static_cast<double *>(h->c.p), N};
-    if ((rc = enqueue_dgemm(h, o, h->mode, st))) {
+    HostOut ho{C, false};
+    if ((rc = enqueue_dgemm(h, o, h->mode, st, -1, 0, kMaxBins, nullptr, &ho))) {
         cudaStreamSynchronize(st);
         return rc;
     }
-    if ((e = cudaMemcpyAsync(C, h->c.p, nC * 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    if (!ho.copied && (e = cudaMemcpyAsync(C, h->c.p, nC * 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
         return cuda_fail(h, e, "copy C");
     return check_device_error(h, st);
 }

@@ -381,7 +381,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                 }
                 return got;
             };
-            for (int t = blockIdx.x; ok && t < g.total_tiles; t += gridDim.x) {
+            for (int t = g.tile_begin + static_cast<int>(blockIdx.x); ok && t < g.total_tiles; t += gridDim.x) {
                 TileRef tr;
                 tile_ref(g, t, &tr);
                 DrainSchedule pds;
@@ -540,7 +540,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
         uint64_t fphase = 0;
         uint32_t prev = 0;
         bool ok = true;
-        for (int t = blockIdx.x; ok && t < g.total_tiles; t += gridDim.x) {
+        for (int t = g.tile_begin + static_cast<int>(blockIdx.x); ok && t < g.total_tiles; t += gridDim.x) {
             TileRef tr;
             tile_ref(g, t, &tr);
 #pragma unroll
@@ -725,7 +725,8 @@ void launch_gemm_variant(const GemmArgs &args, int tiles, size_t smem, void *str
                              opt > static_cast<int>(smem) ? opt : static_cast<int>(smem));
         if (dev >= 0 && dev < 64) raised[dev] = true;
     }
-    const int grid = args.total_tiles < device_sm_count() ? args.total_tiles : device_sm_count();
+    const int range = args.total_tiles - args.tile_begin;
+    const int grid = range < device_sm_count() ? range : device_sm_count();
     (void)tiles;
     kern<<<grid, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(args);
 }

@@ -76,7 +76,8 @@ struct GemmArgs {
     int G;
     int blk_lo[kMaxGroups], blk_nb[kMaxGroups], blk_p0[kMaxGroups], blk_p1[kMaxGroups];
     int blk_period[kMaxGroups], blk_off[kMaxGroups];
-    int total_tiles;  // tiles_m * tiles_n
+    int total_tiles;  // end of the launch's tile range (tiles_m * tiles_n for the whole product)
+    int tile_begin;   // first tile of the launch's range (0 for the whole product)
     int pair_g0;      // OUT_PAIRS: bins in the low word group (the reference's first group)
     // Accumulator groups of the drain: with t = J - 1 - j, bin j is added into the
     // 64-bit accumulator a of its group (the last a with acc_t0[a] <= t) with
