@@ -67,6 +67,7 @@ struct ozgb_context {
     bool have_last = false;
     // buffers
     DevBuf a, b, c, at, bt, er, ec, err, raw, knob, kpart;
+    DevBuf split;  // K-split of a launch's last wave: group sums and counters
     KnobJob kjob{};  // the last stage-(a) statistics, for the precision knob
     DevBuf gstat, gslice, gtab;  // grouped calls: statistics, slice planes, job/problem tables
     cudaStream_t stream = nullptr;       // used by the host-array entry points
@@ -343,6 +344,36 @@ int sm_count(int dev) {
     return cached[dev];
 }
 
+// K-split of the last partial wave of a launch over tiles [begin, end): its R
+// tiles are each split into P K ranges of at least 4 chunks, P <= SMs / R, so
+// that wave fills the SMs; a single-wave launch with fewer tiles than SMs is
+// split the same way.  Sets the GemmArgs split fields (parts 1: no split) and
+// zeroes the scratch.
+ozgb_status set_tail_split(ozgb_handle h, const Plan &p, int begin, int end, cudaStream_t st, GemmArgs *g) {
+    g->tile_begin = begin;
+    g->total_tiles = end;
+    g->split_parts = 1;
+    g->split_start = end;
+    if (g->out_mode != OUT_RN && g->out_mode != OUT_RZ_REF) return OZGB_OK;
+    const int sms = sm_count(h->device), n = end - begin;
+    const int R = n <= sms ? n : n % sms;
+    if (R == 0) return OZGB_OK;
+    const int P = std::min({sms / R, p.n_kc / 4, 16});
+    if (P < 2) return OZGB_OK;
+    const int NA = p.W > 2 ? p.W - 1 : 1;
+    const size_t acc_bytes = static_cast<size_t>(R) * NA * p.BN * BM * 8;
+    const size_t bytes = acc_bytes + static_cast<size_t>(R) * sizeof(int);
+    if (!h->split.ensure(bytes)) return fail(h, OZGB_ERR_ALLOC, "split scratch");
+    cudaError_t e = cudaMemsetAsync(h->split.p, 0, bytes, st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "split scratch");
+    g->split_parts = P;
+    g->split_start = end - R;
+    g->total_tiles = end - R + R * P;
+    g->split_acc = static_cast<unsigned long long *>(h->split.p);
+    g->split_cnt = reinterpret_cast<int *>(static_cast<char *>(h->split.p) + acc_bytes);
+    return OZGB_OK;
+}
+
 // Host destination of C (the host-array entry point, C dense with N columns).
 // When C has more than one group of 8 row tiles, the GEMM runs as two launches:
 // the first covers full waves up to the end of the last group but one, and the
@@ -420,7 +451,7 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
     if (t_split > 0) {
         ozgb_status rc = ensure_aux(h);
         if (rc) return rc;
-        g.total_tiles = t_split;
+        if ((rc = set_tail_split(h, p, 0, t_split, st, &g))) return rc;
         p.fn(g, t_split, p.smem, st);
         cudaEventRecord(h->ev_part, st);
         cudaStreamWaitEvent(h->aux[0], h->ev_part, 0);
@@ -428,8 +459,7 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
         if ((e = cudaMemcpyAsync(ho->C, o.C, n1 * 8, cudaMemcpyDeviceToHost, h->aux[0])) != cudaSuccess)
             return cuda_fail(h, e, "copy C (first rows)");
         cudaEventRecord(h->ev_part_copied, h->aux[0]);
-        g.tile_begin = t_split;
-        g.total_tiles = total;
+        if ((rc = set_tail_split(h, p, t_split, total, st, &g))) return rc;
         p.fn(g, total - t_split, p.smem, st);
         h->launches += 2;
         if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(h, e, "slice-pair GEMM launch");
@@ -443,6 +473,10 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
         cudaStreamWaitEvent(st, h->ev_part_copied, 0);
         ho->copied = true;
         return OZGB_OK;
+    }
+    {
+        const ozgb_status rc = set_tail_split(h, p, 0, total, st, &g);
+        if (rc) return rc;
     }
     p.fn(g, total, p.smem, st);
     h->launches += 1;

@@ -260,9 +260,21 @@ struct TileRef {
     double *c;
     long ldc;
     int M, N, n_kc, mt, nt;
+    int c0, c1;  // chunks of K this work unit covers
+    int split;   // index of the split tile (-1: the unit is a whole tile)
 };
 
-__device__ __forceinline__ void tile_ref(const GemmArgs &g, int t, TileRef *r) {
+__device__ __forceinline__ void tile_ref(const GemmArgs &g, int u, TileRef *r) {
+    int t = u, kpart = 0;
+    r->split = -1;
+    if (g.split_parts > 1 && u >= g.split_start) {
+        const int v = u - g.split_start;
+        r->split = v / g.split_parts;
+        kpart = v - r->split * g.split_parts;
+        t = g.split_start + r->split;
+    }
+    r->c0 = r->split < 0 ? 0 : (kpart * g.n_kc) / g.split_parts;
+    r->c1 = r->split < 0 ? g.n_kc : ((kpart + 1) * g.n_kc) / g.split_parts;
     r->er = g.er;
     r->ec = g.ec;
     r->c = g.c;
@@ -306,7 +318,8 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
     uint64_t *gfull = empty + g.stages;
     uint64_t *gempty = gfull + kMaxGroups;
     uint64_t *mma_done = gempty + kMaxGroups;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mma_done + 1);
+    uint64_t *split_bar = mma_done + 1;  // the drain warps' barrier around a split tile's count
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(split_bar + 1);
     int *abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
     volatile int *vabort = abort_flag;
     // drain mask of the chunk held by each stage (written by the producer before it
@@ -318,6 +331,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
     uint32_t *blk_tm = reinterpret_cast<uint32_t *>(blk_bd + kMaxGroups);   // TMEM address
     uint32_t *blk_id = blk_tm + kMaxGroups;                                 // instruction descriptor
     int *blk_np = reinterpret_cast<int *>(blk_id + kMaxGroups);             // A slices per UMMA run
+    int *split_flag = blk_np + kMaxGroups;  // this CTA's part completed a split tile
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #ifdef OZGB_PROBE
@@ -349,6 +363,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
             mbar_init(&gempty[i], kEpiWarps);
         }
         mbar_init(mma_done, n_iss);
+        mbar_init(split_bar, kEpiWarps);
         *abort_flag = (*reinterpret_cast<volatile int *>(g.err) != 0) ? 1 : 0;
         fence_mbar_init();
     }
@@ -386,13 +401,13 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                 tile_ref(g, t, &tr);
                 DrainSchedule pds;
                 pds.init(g);
-                for (int c = 0; c < tr.n_kc; ++c) {
+                for (int c = tr.c0; c < tr.c1; ++c) {
                     if (*vabort || !acquire()) {
                         ok = false;
                         break;
                     }
                     uint8_t *dst = smem + static_cast<size_t>(st) * g.stage_bytes;
-                    stage_mask[st] = pds.next(g, c == tr.n_kc - 1);  // published by the arrive below
+                    stage_mask[st] = pds.next(g, c == tr.c1 - 1);  // published by the arrive below
                     mbar_arrive_expect_tx(&full[st], g.a_block_bytes + g.b_block_bytes);
                     bulk_g2s(dst, tr.a_src + static_cast<size_t>(c) * g.a_block_bytes, g.a_block_bytes, &full[st]);
                     bulk_g2s(dst + g.a_block_bytes + g.b_pad_lo_bytes,
@@ -540,6 +555,16 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
         uint64_t fphase = 0;
         uint32_t prev = 0;
         bool ok = true;
+        // barrier of the 16 drain warps (one arrival per warp), with the bounded wait
+        // of every other barrier: a warp that gave up cannot leave the others waiting
+        uint32_t sphase = 0;
+        auto drain_bar = [&]() -> bool {
+            __syncwarp();
+            if (lane == 0) mbar_arrive(split_bar);
+            const bool got = mbar_wait(split_bar, sphase, vabort, TO);
+            sphase ^= 1u;
+            return got;
+        };
         for (int t = g.tile_begin + static_cast<int>(blockIdx.x); ok && t < g.total_tiles; t += gridDim.x) {
             TileRef tr;
             tile_ref(g, t, &tr);
@@ -550,8 +575,8 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
 
             DrainSchedule ds;
             ds.init(g);
-            for (int c = 0; ok && c < tr.n_kc; ++c) {
-                const bool last = (c == tr.n_kc - 1);
+            for (int c = tr.c0; ok && c < tr.c1; ++c) {
+                const bool last = (c == tr.c1 - 1);
                 const uint32_t cur = ds.next(g, last);
                 for (int pass = 0; ok && pass < 2; ++pass) {
                     uint32_t m = pass == 0 ? (cur & ~prev) : (cur & prev);
@@ -608,6 +633,41 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                 prev = cur;
             }
             if (!ok) break;
+
+            if (tr.split >= 0) {
+                // a part of a split tile: add the exact group sums into the tile's
+                // scratch (integer adds, exact in any order); the part that completes
+                // the tile's count reads the totals and runs the epilogue
+                unsigned long long *sa = g.split_acc + static_cast<size_t>(tr.split) * (NA * BN * BM);
+                const int rl = 32 * qd + lane;
+#pragma unroll
+                for (int i = 0; i < COLS; ++i)
+#pragma unroll
+                    for (int a = 0; a < NA; ++a)
+                        if (a < g.n_acc)
+                            atomicAdd(sa + (static_cast<size_t>(a) * BN + part * COLS + i) * BM + rl,
+                                      static_cast<unsigned long long>(acc[i][a]));
+                __threadfence();
+                if (!drain_bar()) {
+                    ok = false;
+                    break;
+                }
+                if (ew == 0 && lane == 0)
+                    *split_flag = (atomicAdd(g.split_cnt + tr.split, 1) == g.split_parts - 1) ? 1 : 0;
+                if (!drain_bar()) {
+                    ok = false;
+                    break;
+                }
+                if (!*reinterpret_cast<volatile int *>(split_flag)) continue;
+                __threadfence();
+#pragma unroll
+                for (int i = 0; i < COLS; ++i)
+#pragma unroll
+                    for (int a = 0; a < NA; ++a)
+                        acc[i][a] = a < g.n_acc ? static_cast<long long>(__ldcg(
+                                                      sa + (static_cast<size_t>(a) * BN + part * COLS + i) * BM + rl))
+                                                : 0ll;
+            }
 
             // --------------------------------------------------- epilogue
             OZ_PT(tq);

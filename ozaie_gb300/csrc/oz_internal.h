@@ -78,6 +78,16 @@ struct GemmArgs {
     int blk_period[kMaxGroups], blk_off[kMaxGroups];
     int total_tiles;  // end of the launch's tile range (tiles_m * tiles_n for the whole product)
     int tile_begin;   // first tile of the launch's range (0 for the whole product)
+    // Split of the launch's last partial wave along K: work unit u < split_start is
+    // tile u over all of K; unit u >= split_start is part (u - split_start) %
+    // split_parts of tile split_start + (u - split_start) / split_parts, over chunks
+    // [part n_kc / P, (part + 1) n_kc / P).  Each part adds its 64-bit group sums
+    // into split_acc (per split tile: [NA][BN][128], zero before the launch) and
+    // counts itself in split_cnt; the part that completes the count rounds and
+    // stores the tile.  total_tiles is then the end of the unit range.
+    int split_start, split_parts;
+    unsigned long long *split_acc;
+    int *split_cnt;
     int pair_g0;      // OUT_PAIRS: bins in the low word group (the reference's first group)
     // Accumulator groups of the drain: with t = J - 1 - j, bin j is added into the
     // 64-bit accumulator a of its group (the last a with acc_t0[a] <= t) with

@@ -73,3 +73,18 @@ def test_ill_conditioned_rows(ozlib, oracle):
         sl = slice(64 * i, 64 * (i + 1))
         got = C[rows[sl], cols[sl]]
         assert np.linalg.norm(got - exact[sl]) / np.linalg.norm(exact[sl]) <= 1e-15
+
+
+def test_partial_wave_split_bit_exact(ozlib, oracle):
+    """156 tiles of 128 x 48 on a 152-SM GPU: the last wave's 4 tiles are split
+    into K parts whose exact group sums are added in global memory; every row,
+    including the rows of the split tiles (rows 1152-1663, columns 528-575), keeps
+    the oracle's bits."""
+    M, N, K = 1664, 576, 2048
+    A = oracle.gen_phi((M, K), 47, 1.0)
+    B = oracle.gen_phi((K, N), 48, 1.0)
+    C, cfg = _device_dgemm(ozlib, A, B, 9, 9)
+    assert cfg["tile_n"] == 48
+    for r0 in (0, 700, 1152, 1300, 1663):
+        ref = oracle.dgemm_rows(A, B, 7, 9, 9, 0, r0, r0 + 1)
+        assert np.array_equal(C[r0:r0 + 1].view(np.uint64), ref.view(np.uint64)), r0
