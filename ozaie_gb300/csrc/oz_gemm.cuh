@@ -660,13 +660,19 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                 }
                 if (!*reinterpret_cast<volatile int *>(split_flag)) continue;
                 __threadfence();
+                // the totals, leaving the scratch zero for the next launch
 #pragma unroll
                 for (int i = 0; i < COLS; ++i)
 #pragma unroll
-                    for (int a = 0; a < NA; ++a)
-                        acc[i][a] = a < g.n_acc ? static_cast<long long>(__ldcg(
-                                                      sa + (static_cast<size_t>(a) * BN + part * COLS + i) * BM + rl))
-                                                : 0ll;
+                    for (int a = 0; a < NA; ++a) {
+                        acc[i][a] = 0;
+                        if (a < g.n_acc) {
+                            unsigned long long *ptr = sa + (static_cast<size_t>(a) * BN + part * COLS + i) * BM + rl;
+                            acc[i][a] = static_cast<long long>(__ldcg(ptr));
+                            __stcg(ptr, 0ull);
+                        }
+                    }
+                if (ew == 0 && lane == 0) g.split_cnt[tr.split] = 0;
             }
 
             // --------------------------------------------------- epilogue
