@@ -80,11 +80,24 @@ def test_partial_wave_split_bit_exact(ozlib, oracle):
     into K parts whose exact group sums are added in global memory; every row,
     including the rows of the split tiles (rows 1152-1663, columns 528-575), keeps
     the oracle's bits."""
+    import torch
     M, N, K = 1664, 576, 2048
     A = oracle.gen_phi((M, K), 47, 1.0)
     B = oracle.gen_phi((K, N), 48, 1.0)
-    C, cfg = _device_dgemm(ozlib, A, B, 9, 9)
-    assert cfg["tile_n"] == 48
-    for r0 in (0, 700, 1152, 1300, 1663):
-        ref = oracle.dgemm_rows(A, B, 7, 9, 9, 0, r0, r0 + 1)
-        assert np.array_equal(C[r0:r0 + 1].view(np.uint64), ref.view(np.uint64)), r0
+    dev = torch.device("cuda", 0)
+    dA, dB = torch.from_numpy(A).to(dev), torch.from_numpy(B).to(dev)
+    h = ozlib.Handle()
+    h.set_slices(9)
+    h.set_bins(9)
+    refs = {r0: oracle.dgemm_rows(A, B, 7, 9, 9, 0, r0, r0 + 1) for r0 in (0, 700, 1152, 1300, 1663)}
+    # three calls on one handle: the later ones use the scratch the earlier ones left zero
+    for _ in range(3):
+        dC = torch.full((M, N), float("nan"), dtype=torch.float64, device=dev)
+        assert h.dgemm_device(M, N, K, dA.data_ptr(), K, dB.data_ptr(), N, dC.data_ptr(), N,
+                              torch.cuda.current_stream().cuda_stream) == 0, h.last_error()
+        assert h.sync() == 0, h.last_error()
+        assert h.config()["tile_n"] == 48
+        C = dC.cpu().numpy()
+        for r0, ref in refs.items():
+            assert np.array_equal(C[r0:r0 + 1].view(np.uint64), ref.view(np.uint64)), r0
+    h.close()
