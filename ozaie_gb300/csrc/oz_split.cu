@@ -437,6 +437,21 @@ __device__ __forceinline__ void unit_sq_warp(const StatParts &sp, int u, int lan
     *s = v;
 }
 
+// Combined (E, s) of unit u by one thread, for units with few partials: the
+// loads of many units are in flight at once instead of one unit per warp.
+__device__ __forceinline__ void unit_sq_thread(const StatParts &sp, int u, int *E, float *s) {
+    int e = 0;
+    float v = 0.0f;
+    const unsigned long long *p = sp.p + u * sp.unit_stride;
+#pragma unroll 4
+    for (int i = 0; i < sp.nparts; ++i) {
+        const unsigned long long w = __ldg(p + i * sp.part_stride);
+        sq_merge(e, v, static_cast<int>(w >> 32), __uint_as_float(static_cast<uint32_t>(w)));
+    }
+    *E = e;
+    *s = v;
+}
+
 // Part `chunk` of `chunks` of one of the three knob sums (role 0: A terms, 1: B
 // terms, 2: the k-direction term), added atomically into j.out (zeroed before);
 // one warp per unit.  With ea, eb the largest row / column exponents of op(A) /
@@ -460,23 +475,46 @@ __device__ __forceinline__ void knob_stats_body(const KnobJob &j, const int role
     const int per = (n + chunks - 1) / chunks;
     const int i0 = chunk * per, i1 = min(n, i0 + per);
     double num = 0.0, den = 0.0, t = 0.0;
-    for (int u = i0 + wid; u < i1; u += nw) {
-        if (role < 2) {
-            const StatParts &sp = role == 0 ? j.ra : j.cb;
-            const int emax = role == 0 ? ea : eb;
-            int E;
-            float sq;
-            unit_sq_warp(sp, u, lane, &E, &sq);
-            if (lane == 0) {
+    const int nparts = role == 0 ? j.ra.nparts : (role == 1 ? j.cb.nparts : max(j.ka.nparts, j.kb.nparts));
+    if (nparts <= 32) {
+        // one thread per unit
+        for (int u = i0 + static_cast<int>(threadIdx.x); u < i1; u += blockDim.x) {
+            if (role < 2) {
+                const StatParts &sp = role == 0 ? j.ra : j.cb;
+                const int emax = role == 0 ? ea : eb;
+                int E;
+                float sq;
+                unit_sq_thread(sp, u, &E, &sq);
                 num += pow2i(2 * ((role == 0 ? j.er[u] : j.ec[u]) - emax));
                 den += scale2(static_cast<double>(sq), 2 * (E - emax) - 2);
+            } else {
+                int E1, E2;
+                float s1, s2;
+                unit_sq_thread(j.ka, u, &E1, &s1);
+                unit_sq_thread(j.kb, u, &E2, &s2);
+                t += scale2(static_cast<double>(s1) * s2, 2 * (E1 + E2 - ea - eb - 2));
             }
-        } else {
-            int E1, E2;
-            float s1, s2;
-            unit_sq_warp(j.ka, u, lane, &E1, &s1);
-            unit_sq_warp(j.kb, u, lane, &E2, &s2);
-            if (lane == 0) t += scale2(static_cast<double>(s1) * s2, 2 * (E1 + E2 - ea - eb - 2));
+        }
+    } else {
+        // one warp per unit
+        for (int u = i0 + wid; u < i1; u += nw) {
+            if (role < 2) {
+                const StatParts &sp = role == 0 ? j.ra : j.cb;
+                const int emax = role == 0 ? ea : eb;
+                int E;
+                float sq;
+                unit_sq_warp(sp, u, lane, &E, &sq);
+                if (lane == 0) {
+                    num += pow2i(2 * ((role == 0 ? j.er[u] : j.ec[u]) - emax));
+                    den += scale2(static_cast<double>(sq), 2 * (E - emax) - 2);
+                }
+            } else {
+                int E1, E2;
+                float s1, s2;
+                unit_sq_warp(j.ka, u, lane, &E1, &s1);
+                unit_sq_warp(j.kb, u, lane, &E2, &s2);
+                if (lane == 0) t += scale2(static_cast<double>(s1) * s2, 2 * (E1 + E2 - ea - eb - 2));
+            }
         }
     }
     if (role < 2) {
@@ -597,7 +635,7 @@ void launch_stage_jobs(const StageJob *jobs, const int *block0, int n_jobs, int 
 }
 
 void launch_knob_grouped(const KnobJob *jobs, int n, void *stream) {
-    if (n > 0) k_knob_grouped<<<3 * n, 1024, 0, static_cast<cudaStream_t>(stream)>>>(jobs);
+    if (n > 0) k_knob_grouped<<<3 * n, 256, 0, static_cast<cudaStream_t>(stream)>>>(jobs);
 }
 
 void launch_knob_stats(const KnobJob &j, void *stream) {
