@@ -349,12 +349,18 @@ __device__ __forceinline__ void stats2d_body(const double *__restrict__ X, long 
     const bool rows_wanted = row_e || row_part;
     int Ec = 0;
     float sc = 0.0f;
+    // the next chunk's rows are loaded before this chunk's reduction and barriers
+    double x[RB], xn[RB];
+#pragma unroll
+    for (int u = 0; u < RB; ++u) {
+        const int r = r0 + u;
+        x[u] = (cin && r < rows) ? __ldg(X + static_cast<size_t>(r) * ld + c) : 0.0;
+    }
     for (int i0 = 0; i0 < kStatsRows; i0 += RB) {
-        double x[RB];
 #pragma unroll
         for (int u = 0; u < RB; ++u) {
-            const int r = r0 + i0 + u;
-            x[u] = (cin && r < rows) ? __ldg(X + static_cast<size_t>(r) * ld + c) : 0.0;
+            const int r = r0 + i0 + RB + u;
+            xn[u] = (cin && i0 + RB < kStatsRows && r < rows) ? __ldg(X + static_cast<size_t>(r) * ld + c) : 0.0;
         }
 #pragma unroll
         for (int u = 0; u < RB; ++u) {
@@ -388,6 +394,8 @@ __device__ __forceinline__ void stats2d_body(const double *__restrict__ X, long 
             }
             __syncthreads();
         }
+#pragma unroll
+        for (int u = 0; u < RB; ++u) x[u] = xn[u];
     }
     if (rows_wanted) {
         const int r = r0 + static_cast<int>(threadIdx.x);
