@@ -415,6 +415,67 @@ def mix_run(n, dev, stream, oz, O, torch):
                                         "adaptive_err", "plain_err", "cublas_err"], "rows": per}}
 
 
+def sweep_run(dev, stream, oz, O, torch):
+    """The square workload's full grid: M = N = K = 4096, both pair sets (fast:
+    triangular, accurate: full), s = 3..8 slices of 7 bits, phi in {0.5, 1, 2, 4}
+    (A seed 1, B seed 2).  Errors on 1000 sampled entries against the exact
+    products and MPFR-106 (the reference's oracle), and normwise over all of C
+    against a 16-slice product; cuBLAS FP64 beside each phi."""
+    rows = []
+    n = 4096
+    for phi in (0.5, 1.0, 2.0, 4.0):
+        A = O.gen_phi((n, n), 1, phi)
+        B = O.gen_phi((n, n), 2, phi)
+        dA, dB = torch.from_numpy(A).to(dev), torch.from_numpy(B).to(dev)
+        dC = torch.empty((n, n), dtype=torch.float64, device=dev)
+        dR = torch.empty_like(dC)
+        r, c = O.sample_indices(n, n, 1000, 3)
+        exact, absdot = O.exact_entries(A, B, r, c)
+        mp = O.mpfr_entries(A, B, r, c)
+        hr = oz.Handle()
+        hr.set_slices(16)
+        hr.set_bins(16)
+        if hr.dgemm_device(n, n, n, dA.data_ptr(), n, dB.data_ptr(), n, dR.data_ptr(), n, stream.cuda_stream):
+            raise RuntimeError(hr.last_error())
+        hr.close()
+        rn = torch.linalg.norm(dR).item()
+
+        def errs(C):
+            got = C[r, c]
+            e = {"sampled_normwise_vs_exact": float(np.linalg.norm(got - exact) / np.linalg.norm(exact)),
+                 "sampled_max_componentwise": float(np.max(np.abs(got - exact) / np.maximum(absdot, 1e-300)))}
+            if mp is not None:
+                e["sampled_normwise_vs_mpfr106"] = float(np.linalg.norm(got - mp) / np.linalg.norm(mp))
+            return e
+
+        ms = time_device(lambda: torch.matmul(dA, dB, out=dC), torch, stream, 1)
+        e = errs(dC.cpu().numpy())
+        e["normwise_all_vs_16_slices"] = torch.linalg.norm(dC - dR).item() / rn
+        rows.append({"phi": phi, "impl": "cublas_dgemm", "ms": ms, "tflops": 2.0 * n ** 3 / ms / 1e9, **e})
+        for mode in ("fast", "accurate"):
+            for sl in range(3, 9):
+                h = oz.Handle()
+                h.set_slices(sl)
+                h.set_bins(sl if mode == "fast" else 2 * sl - 1)
+
+                def call():
+                    if h.dgemm_device(n, n, n, dA.data_ptr(), n, dB.data_ptr(), n, dC.data_ptr(), n,
+                                      stream.cuda_stream):
+                        raise RuntimeError(h.last_error())
+
+                call()
+                ms = time_device(call, torch, stream, 3)
+                if h.sync():
+                    raise RuntimeError(h.last_error())
+                h.close()
+                e = errs(dC.cpu().numpy())
+                e["normwise_all_vs_16_slices"] = torch.linalg.norm(dC - dR).item() / rn
+                rows.append({"phi": phi, "impl": "ozaki_%s_s%d" % (mode, sl), "ms": ms,
+                             "tflops": 2.0 * n ** 3 / ms / 1e9, **e})
+        del dA, dB, dC, dR
+    return {"workload": "M = N = K = 4096, a = (U - 0.5) exp(phi N), A seed 1, B seed 2", "rows": rows}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -460,6 +521,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="use the planner's cost-model plans")
     ap.add_argument("--longk", action="store_true", help="add the long-K workload (8192^2 x 65536, ~1 min)")
     ap.add_argument("--mix", type=int, default=0, help="add the accuracy-adaptive mix of this many problems")
+    ap.add_argument("--sweep", action="store_true",
+                    help="add the 4096^3 grid: both pair sets, s = 3..8, phi in {0.5, 1, 2, 4} (~1 min)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -615,6 +678,7 @@ def main():
     batched = batched_run(args.batched, dev, stream, oz, O, torch) if args.batched > 0 and rank == 0 else None
     long_k = long_k_run(dev, stream, oz, O, torch) if args.longk and rank == 0 else None
     mix = mix_run(args.mix, dev, stream, oz, O, torch) if args.mix > 0 and rank == 0 else None
+    sweep = sweep_run(dev, stream, oz, O, torch) if args.sweep and rank == 0 else None
 
     peaks = load_peaks()
     mma_flops = 2.0 * cfg["pairs"] * M * N * K
@@ -648,6 +712,7 @@ def main():
             "batched": batched,
             "long_k": long_k,
             "adaptive_mix": mix,
+            "sweep_4096": sweep,
             "autotuned": {s: {k: v for k, v in c.items() if k in ("tile_n", "k_chunk", "stages", "blocks", "block_lo",
                                                                  "block_nb", "issuers")} for s, c in tuned.items()}
             if tuned else None,
