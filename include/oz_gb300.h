@@ -74,6 +74,7 @@ typedef struct {
     int block_lo[8]; /* first bin of each block */
     int block_nb[8]; /* bins in each block */
     int issuers;     /* threads issuing the UMMAs (bin blocks split between them) */
+    int slice_format;/* 0: bf16 slices (kind::f16); 1: e4m3 slices (kind::f8f6f4, b <= 4) */
 } ozgb_config;
 
 /* ---------------------------------------------------------------- handles */

@@ -29,6 +29,7 @@ class OzgbConfig(ctypes.Structure):
         ("block_lo", ctypes.c_int * 8),
         ("block_nb", ctypes.c_int * 8),
         ("issuers", ctypes.c_int),
+        ("slice_format", ctypes.c_int),
     ]
 
     def as_dict(self):

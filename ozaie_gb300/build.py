@@ -19,6 +19,7 @@ SOURCES = [
     "oz_gemm_v2.cu",
     "oz_gemm_v3.cu",
     "oz_gemm_v4.cu",
+    "oz_gemm_v5.cu",
     "oz_split.cu",
     "oz_capi.cu",
     "oz_noalloc.cu",

@@ -414,13 +414,13 @@ struct HostOut {
 // Stages (b) and (c)+(d) for one problem whose exponents are in h->er / h->ec.
 ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, int out_mode, int32_t *raw,
                                cudaStream_t st, HostOut *ho = nullptr) {
-    if (!h->at.ensure(p.a_elems * 2) || !h->bt.ensure(p.b_elems * 2))
+    if (!h->at.ensure(p.a_bytes) || !h->bt.ensure(p.b_bytes))
         return fail(h, OZGB_ERR_ALLOC, "slice buffers");
     uint16_t *at = static_cast<uint16_t *>(h->at.p), *bt = static_cast<uint16_t *>(h->bt.p);
     launch_split_a(o.A, o.lda, o.M, o.K, static_cast<int32_t *>(h->er.p), p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.Mp, at, st,
-                   o.ta);
+                   o.ta, p.f8);
     launch_split_b(o.B, o.ldb, o.K, o.N, static_cast<int32_t *>(h->ec.p), p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.BN, p.Np,
-                   bt, st, o.tb);
+                   bt, st, o.tb, p.f8);
     h->launches += 2;
     if (h->profiling) cudaEventRecord(h->ev[2], st);
     GemmArgs g;
@@ -539,6 +539,8 @@ ozgb_status enqueue_dgemm(ozgb_handle h, const Operands &o, int mode, cudaStream
     if (h->profiling) cudaEventRecord(h->ev[1], st);
     OzConfig cfg;
     if ((rc = choose_config(h, o, mode, st, &cfg))) return rc;
+    // dumps read the slice planes back as bf16
+    if (out_mode_override == OUT_RAW || out_mode_override == OUT_PAIRS) cfg.carrier = 1;
     Plan p;
     std::string why;
     PlanHints pairs_hint;
@@ -798,9 +800,9 @@ ozgb_status enqueue_grouped(ozgb_handle h, ozgb_problem *probs, int n, int mode,
     size_t sl_total = 0;
     for (int i = 0; i < n; ++i) {
         a_off[i] = sl_total;
-        sl_total += align256(plans[i].a_elems * 2);
+        sl_total += align256(plans[i].a_bytes);
         b_off[i] = sl_total;
-        sl_total += align256(plans[i].b_elems * 2);
+        sl_total += align256(plans[i].b_bytes);
     }
     if (!h->gslice.ensure(sl_total)) return fail(h, OZGB_ERR_ALLOC, "grouped slice buffer");
     uint8_t *gsl = static_cast<uint8_t *>(h->gslice.p);
@@ -822,6 +824,7 @@ ozgb_status enqueue_grouped(ozgb_handle h, ozgb_problem *probs, int n, int mode,
         j.kind = JOB_SPLIT_A, j.X = pb.A, j.ld = pb.lda, j.rows = pb.M, j.cols = pb.K;
         j.e_in = reinterpret_cast<int32_t *>(at(so[i].er));
         j.b = p.cfg.b, j.s = p.cfg.s, j.KC = p.KC, j.n_kc = p.n_kc, j.padded = p.Mp, j.BN = p.BN;
+        j.f8 = p.f8 ? 1 : 0;
         j.tiles = reinterpret_cast<uint16_t *>(gsl + a_off[i]);
         jb.add(j);
         j.kind = JOB_SPLIT_B, j.X = pb.B, j.ld = pb.ldb, j.rows = pb.K, j.cols = pb.N;
@@ -896,6 +899,7 @@ void fill_blocks(const Plan &p, ozgb_config *out) {
     out->blocks = p.G;
     out->umma_per_kstep = p.mma_per_kstep;
     out->issuers = p.n_iss;
+    out->slice_format = p.f8 ? 1 : 0;
     for (int i = 0; i < 8; ++i) {
         out->block_lo[i] = i < p.G ? p.blk_lo[i] : 0;
         out->block_nb[i] = i < p.G ? p.blk_nb[i] : 0;
@@ -966,8 +970,8 @@ ozgb_status ozgb_setup(ozgb_handle h, int M, int N, int K, int mode) {
     std::string why;
     if (!make_plan(M, N, K, cfg, &p, &why)) return fail(h, OZGB_ERR_UNSUPPORTED, why);
     const size_t nA = static_cast<size_t>(M) * K, nB = static_cast<size_t>(K) * N, nC = static_cast<size_t>(M) * N;
-    if (!h->a.ensure(nA * 8) || !h->b.ensure(nB * 8) || !h->c.ensure(nC * 8) || !h->at.ensure(p.a_elems * 2) ||
-        !h->bt.ensure(p.b_elems * 2) || !h->er.ensure(4 * M) || !h->ec.ensure(4 * N))
+    if (!h->a.ensure(nA * 8) || !h->b.ensure(nB * 8) || !h->c.ensure(nC * 8) || !h->at.ensure(p.a_bytes) ||
+        !h->bt.ensure(p.b_bytes) || !h->er.ensure(4 * M) || !h->ec.ensure(4 * N))
         return fail(h, OZGB_ERR_ALLOC, "device buffers for the setup shape");
     h->M = M;
     h->N = N;
@@ -1338,10 +1342,12 @@ ozgb_status ozgb_autotune(ozgb_handle h, int M, int N, int K, int bits, int slic
         Plan p;
         std::string why;
         if (!make_plan(M, N, K, cfg, &p, &why, 0, 1 << 30, &cands[i])) continue;
-        if (!h->at.ensure(p.a_elems * 2) || !h->bt.ensure(p.b_elems * 2)) continue;
+        if (!h->at.ensure(p.a_bytes) || !h->bt.ensure(p.b_bytes)) continue;
         uint16_t *at = static_cast<uint16_t *>(h->at.p), *bt = static_cast<uint16_t *>(h->bt.p);
-        launch_split_a(dA, K, M, K, static_cast<int32_t *>(h->er.p), p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.Mp, at, st);
-        launch_split_b(dB, N, K, N, static_cast<int32_t *>(h->ec.p), p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.BN, p.Np, bt, st);
+        launch_split_a(dA, K, M, K, static_cast<int32_t *>(h->er.p), p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.Mp, at, st,
+                       false, p.f8);
+        launch_split_b(dB, N, K, N, static_cast<int32_t *>(h->ec.p), p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.BN, p.Np, bt, st,
+                       false, p.f8);
         GemmArgs g;
         gemm_args_from_plan(&g, p, OUT_RN, static_cast<int *>(h->err.p), h->timeout_ns);
         g.a_tiles = at;

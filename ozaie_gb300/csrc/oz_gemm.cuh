@@ -302,7 +302,7 @@ constexpr uint32_t kStageTerminate = 0x80000000u;
 // the next tile's first chunks and the UMMAs of the next tile start as soon as
 // each block's final drain of the previous tile has read it out, while the
 // drain warps round and store the previous tile.
-template <int BN, int W, int KC>
+template <int BN, int W, int KC, bool F8>
 __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_constant__ GemmArgs g) {
     constexpr int PARTS = kEpiWarps / 4;          // drain warps sharing one TMEM lane quadrant
     constexpr int COLS = BN / PARTS;              // columns per drain thread
@@ -449,7 +449,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                 const uint32_t a0 = smem_u32(smem);
                 const uint64_t ad0 = smem_desc(a0, 128, sbo);
                 const uint64_t bd0 = smem_desc(a0 + g.a_block_bytes + g.b_pad_lo_bytes, 128, sbo);
-                const uint32_t idesc_base = idesc_bf16_f32(BM, 16) & ~(0x3Fu << 17);
+                const uint32_t idesc_base = (F8 ? idesc_e4m3_f32(BM, 16) : idesc_bf16_f32(BM, 16)) & ~(0x3Fu << 17);
 #pragma unroll
                 for (int i = 0; i < kMaxGroups; ++i) {
                     if (i < g.G && ((mine >> i) & 1u)) {
@@ -511,8 +511,13 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                         for (int p = 0; p < np; ++p) {
 #pragma unroll
                             for (int kk = 0; kk < ksteps; ++kk) {
-                                umma_bf16(d_tmem, ad + static_cast<uint64_t>(kk * 16),
-                                          bd + static_cast<uint64_t>(kk * 16), idesc, acc);
+                                // one UMMA covers 32 bytes of K per row: 16 bf16 or 32 e4m3 values
+                                if constexpr (F8)
+                                    umma_e4m3(d_tmem, ad + static_cast<uint64_t>(kk * 16),
+                                              bd + static_cast<uint64_t>(kk * 16), idesc, acc);
+                                else
+                                    umma_bf16(d_tmem, ad + static_cast<uint64_t>(kk * 16),
+                                              bd + static_cast<uint64_t>(kk * 16), idesc, acc);
                                 acc = 1u;
                             }
                             ad += a_step;
@@ -775,9 +780,11 @@ inline int device_sm_count() {
     return cached[dev];
 }
 
-template <int BN, int W, int KC>
+// F8: e4m3 slices (kind::f8f6f4); KC is then the bf16-equivalent chunk (bytes / 2
+// per row and slice), i.e. half the K values the chunk holds.
+template <int BN, int W, int KC, bool F8 = false>
 void launch_gemm_variant(const GemmArgs &args, int tiles, size_t smem, void *stream) {
-    auto kern = oz_gemm_kernel<BN, W, KC>;
+    auto kern = oz_gemm_kernel<BN, W, KC, F8>;
     // the shared-memory limit is raised once per device to the opt-in maximum (a
     // per-launch attribute call costs more than the launch itself; every caller
     // sets the same value, so concurrent first calls do not conflict)

@@ -44,6 +44,11 @@ constexpr size_t kCtrlBytes = 1024 + 1024;
 OZ_HD inline long canon_offset(int r, int kk, int KC) {
     return (long)(((r >> 3) * (KC >> 3) + (kk >> 3)) * 64 + (r & 7) * 8 + (kk & 7));
 }
+// The same layout for one-byte (e4m3) slices: 16 K values per core-matrix row, so a
+// 64-deep e4m3 chunk has the byte layout of a 32-deep bf16 chunk.
+OZ_HD inline long canon_offset8(int r, int kk, int KC) {
+    return (long)(((r >> 3) * (KC >> 4) + (kk >> 4)) * 128 + (r & 7) * 16 + (kk & 15));
+}
 
 struct GemmArgs {
     const uint16_t *a_tiles;
@@ -125,6 +130,7 @@ struct StageJob {
     double *ss_out;      // ROWMAX / COLMAX: sums of squares (may be null)
     const int32_t *e_in; // SPLIT: row (A) / column (B) exponents
     int b, s, KC, n_kc, padded, BN;  // SPLIT: padded = Mp (A) or Np (B)
+    int f8;                          // SPLIT: e4m3 slices (b <= 4)
     uint16_t *tiles;
     int32_t *e_out2;                  // STATS: column exponent fields (atomic max, may be null)
     unsigned long long *prow, *pcol;  // STATS: row partials [rows][ceil(cols/256)], column partials [ceil(rows/64)][cols]
@@ -159,15 +165,21 @@ typedef void (*GemmLaunchFn)(const GemmArgs &args, int grid, size_t smem, void *
     X(16, 4, 32) X(16, 4, 16) X(16, 5, 32) X(16, 5, 16)
 #define OZ_DECLARE_GEMM(BN, W, KC) void launch_gemm_##BN##_##W##_##KC(const GemmArgs &, int, size_t, void *);
 OZ_GEMM_VARIANTS(OZ_DECLARE_GEMM)
+// e4m3-carrier variants (b <= 4), KC in bf16-equivalent units (a 64-deep e4m3 chunk)
+#define OZ_GEMM_F8_VARIANTS(X) \
+    X(64, 3, 32) X(32, 3, 32) X(32, 4, 32) X(16, 4, 32) X(16, 5, 32) X(32, 3, 16) X(32, 4, 16) X(16, 4, 16) X(16, 5, 16)
+#define OZ_DECLARE_GEMM_F8(BN, W, KC) void launch_gemm_f8_##BN##_##W##_##KC(const GemmArgs &, int, size_t, void *);
+OZ_GEMM_F8_VARIANTS(OZ_DECLARE_GEMM_F8)
 
 // Stage (a) / (b) launches (oz_split.cu).
 void launch_rowmax(const double *A, long lda, int M, int K, int32_t *er, double *ss, void *stream);
 void launch_colmax(const double *B, long ldb, int K, int N, int32_t *ec, double *ss, void *stream);
 // trans: A is stored K x M (element (m, k) at A[k * lda + m]); B is stored N x K.
+// f8: one-byte e4m3 slices (b <= 4), in the byte layout of a bf16 block of half the K chunk.
 void launch_split_a(const double *A, long lda, int M, int K, const int32_t *er, int b, int s, int KC, int n_kc,
-                    int Mp, uint16_t *tiles, void *stream, bool trans = false);
+                    int Mp, uint16_t *tiles, void *stream, bool trans = false, bool f8 = false);
 void launch_split_b(const double *B, long ldb, int K, int N, const int32_t *ec, int b, int s, int KC, int n_kc,
-                    int BN, int Np, uint16_t *tiles, void *stream, bool trans = false);
+                    int BN, int Np, uint16_t *tiles, void *stream, bool trans = false, bool f8 = false);
 int launch_selftest_timeout(int *err, unsigned long long timeout_ns, void *stream);
 // One pass over a row-major rows x cols operand: exponent maxima of its rows
 // and/or columns (atomic max into row_e / col_e, zeroed before; either may be

@@ -91,8 +91,8 @@ extern "C" ozgb_status ozgb_dgemm_device_noalloc(int M, int N, int K, const doub
     const size_t off_er = 256;
     const size_t off_ec = off_er + round256(sizeof(int32_t) * M);
     const size_t off_at = off_ec + round256(sizeof(int32_t) * N);
-    const size_t off_bt = off_at + round256(p.a_elems * 2);
-    const size_t need = off_bt + round256(p.b_elems * 2);
+    const size_t off_bt = off_at + round256(p.a_bytes);
+    const size_t need = off_bt + round256(p.b_bytes);
     if (need > kNoAllocScratchBytes) return OZGB_ERR_TOO_LARGE;
 
     unsigned char *base = nullptr;
@@ -113,8 +113,8 @@ extern "C" ozgb_status ozgb_dgemm_device_noalloc(int M, int N, int K, const doub
     }
     launch_rowmax(dA, lda, M, K, er, nullptr, st);
     launch_colmax(dB, ldb, K, N, ec, nullptr, st);
-    launch_split_a(dA, lda, M, K, er, p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.Mp, at, st);
-    launch_split_b(dB, ldb, K, N, ec, p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.BN, p.Np, bt, st);
+    launch_split_a(dA, lda, M, K, er, p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.Mp, at, st, false, p.f8);
+    launch_split_b(dB, ldb, K, N, ec, p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.BN, p.Np, bt, st, false, p.f8);
 
     GemmArgs g;
     std::memset(&g, 0, sizeof g);

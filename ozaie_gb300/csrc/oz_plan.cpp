@@ -14,14 +14,16 @@ namespace ozgb {
 namespace {
 
 struct Variant {
-    int BN, W, KC;
+    int BN, W, KC;  // KC: the kernel's chunk in bf16-equivalent units (K values for bf16, half of them for e4m3)
+    bool f8;
     GemmLaunchFn fn;
 };
 
-#define OZ_VARIANT_ENTRY(BN, W, KC) {BN, W, KC, launch_gemm_##BN##_##W##_##KC},
+#define OZ_VARIANT_ENTRY(BN, W, KC) {BN, W, KC, false, launch_gemm_##BN##_##W##_##KC},
+#define OZ_VARIANT_ENTRY_F8(BN, W, KC) {BN, W, KC, true, launch_gemm_f8_##BN##_##W##_##KC},
 // Kernel variants, largest tile first.  BN * J <= 512 TMEM columns and the
-// drain registers (BN/2 * W words) bound which ones exist.
-const Variant kVariants[] = {OZ_GEMM_VARIANTS(OZ_VARIANT_ENTRY)};
+// drain registers (2 (W-1) words per column) bound which ones exist.
+const Variant kVariants[] = {OZ_GEMM_VARIANTS(OZ_VARIANT_ENTRY) OZ_GEMM_F8_VARIANTS(OZ_VARIANT_ENTRY_F8)};
 
 constexpr size_t kSmemLimit = 232448;  // max dynamic shared memory per block on sm_103
 constexpr size_t kSmemReserve = kCtrlBytes;
@@ -55,7 +57,7 @@ void reference_table(int K, int mode, int *b, int *d) {
 }
 
 namespace {
-using TuneKey = std::tuple<int, int, int, int, int, int, int>;
+using TuneKey = std::tuple<int, int, int, int, int, int, int, int>;
 std::mutex g_tune_mu;
 std::map<TuneKey, PlanHints> g_tune;
 long g_tune_generation = 0;  // bumped whenever the table changes (plans cached under the old one are stale)
@@ -66,7 +68,7 @@ int ceil_log2(int x) {
     return l;
 }
 TuneKey tune_key(int M, int N, int K, const OzConfig &cfg) {
-    return TuneKey{cfg.b, cfg.s, cfg.J, cfg.rounding, ceil_log2(M), ceil_log2(N), ceil_log2(K)};
+    return TuneKey{cfg.b, cfg.s, cfg.J, cfg.rounding, cfg.carrier, ceil_log2(M), ceil_log2(N), ceil_log2(K)};
 }
 }  // namespace
 
@@ -100,7 +102,7 @@ bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std
 namespace {
 // Plans without hints are pure functions of the shape, the configuration and the
 // tuning table: cached, so that grouped calls with many problems plan in O(1) each.
-using PlanKey = std::tuple<int, int, int, int, int, int, int, int, int, long>;
+using PlanKey = std::tuple<int, int, int, int, int, int, int, int, int, int, long>;
 std::mutex g_plan_mu;
 std::map<PlanKey, Plan> g_plans;
 }  // namespace
@@ -114,7 +116,7 @@ bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string 
         std::lock_guard<std::mutex> lk(g_tune_mu);
         gen = g_tune_generation;
     }
-    const PlanKey key{M, N, K, cfg.b, cfg.s, cfg.J, cfg.rounding, bin_lo, std::min(bin_hi, 1 << 20), gen};
+    const PlanKey key{M, N, K, cfg.b, cfg.s, cfg.J, cfg.rounding, cfg.carrier, bin_lo, std::min(bin_hi, 1 << 20), gen};
     {
         std::lock_guard<std::mutex> lk(g_plan_mu);
         auto it = g_plans.find(key);
@@ -212,17 +214,24 @@ bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std
             gsum = one;
         }
     }
-    const Variant *chosen = nullptr;
-    for (const Variant &v : kVariants) {
-        if (v.KC != 32) continue;
-        if (hint.BN && v.BN != hint.BN) continue;
-        if (v.W < hint.min_W) continue;
-        if (std::max(1, v.W - 1) < n_acc) continue;  // accumulator groups the variant holds
-        if (v.BN * J > 512) continue;
-        if (32 * v.W < bits) continue;
-        chosen = &v;
-        break;
-    }
+    // Carrier: e4m3 holds every slice of b <= 4 bits (|v| <= 15) exactly and one
+    // kind::f8f6f4 UMMA covers 32 K values, twice a bf16 UMMA's, for about the same
+    // time; bf16 otherwise, or when the planes are read back as bf16.
+    auto pick = [&](bool f8) -> const Variant * {
+        for (const Variant &v : kVariants) {
+            if (v.f8 != f8 || v.KC != 32) continue;
+            if (hint.BN && v.BN != hint.BN) continue;
+            if (v.W < hint.min_W) continue;
+            if (std::max(1, v.W - 1) < n_acc) continue;  // accumulator groups the variant holds
+            if (v.BN * J > 512) continue;
+            if (32 * v.W < bits) continue;
+            return &v;
+        }
+        return nullptr;
+    };
+    const Variant *chosen = (b <= 4 && cfg.carrier != 1 && kb_max >= 64) ? pick(true) : nullptr;
+    p.f8 = chosen != nullptr;
+    if (!chosen) chosen = pick(false);
     if (!chosen) {
         *err = "no kernel variant holds " + std::to_string(J) + " bins with a " + std::to_string(bits) +
                "-bit exact accumulator";
@@ -383,19 +392,22 @@ bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std
     // two issuing threads (bin blocks split by parity) unless the hint says one
     p.n_iss = (p.G >= 2 && hint.issuers != 1) ? 2 : 1;
 
-    // ---- pipeline: K chunk and stage count
+    // ---- pipeline: K chunk and stage count (a chunk of 32 bf16 or 64 e4m3 K values
+    // is 64 bytes per row and slice)
+    const size_t eb = p.f8 ? 1 : 2;
     const size_t budget = kSmemLimit - kSmemReserve;
-    const int kc_opts[2] = {32, 16};
+    const int kc_opts[2] = {p.f8 ? 64 : 32, p.f8 ? 32 : 16};
+    const int kmin = kc_opts[1];
     const char *env_kc = std::getenv("OZGB_KC");  // tuning override
     const int force_kc = hint.KC ? hint.KC : (env_kc ? std::atoi(env_kc) : 0);
     auto stage_of = [&](int kc) {
-        return static_cast<size_t>(s) * BM * kc * 2 + static_cast<size_t>(p.pad_lo + s + p.pad_hi) * p.BN * kc * 2;
+        return (static_cast<size_t>(s) * BM * kc + static_cast<size_t>(p.pad_lo + s + p.pad_hi) * p.BN * kc) * eb;
     };
     p.KC = 0;
     for (int kc : kc_opts) {
         if (force_kc && kc != force_kc) continue;
         if (kc > kb_max) continue;
-        if (kc > 16 && kc > ((K + 15) / 16) * 16) continue;  // no wider than K needs
+        if (kc > kmin && kc > ((K + kmin - 1) / kmin) * kmin) continue;  // no wider than K needs
         const size_t st = budget / stage_of(kc);
         if (st >= 2) {
             p.KC = kc;
@@ -405,16 +417,23 @@ bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std
         }
     }
     if (!p.KC) {
-        if (stage_of(16) > budget) {
-            *err = "slices do not fit one 16-deep pipeline stage in shared memory";
+        if (stage_of(kmin) > budget) {
+            *err = "slices do not fit one pipeline stage in shared memory";
             return false;
         }
-        p.KC = 16;
+        p.KC = kmin;
         p.stages = 1;
     }
     p.fn = nullptr;
+    const int vkc = p.f8 ? p.KC / 2 : p.KC;  // the kernel's bf16-equivalent chunk
     for (const Variant &v : kVariants)
-        if (v.BN == p.BN && v.W == p.W && v.KC == p.KC) p.fn = v.fn;
+        if (v.f8 == p.f8 && v.BN == p.BN && v.W == p.W && v.KC == vkc) p.fn = v.fn;
+    if (!p.fn && p.f8) {
+        // no e4m3 kernel for this tile / accumulator / chunk: the same with bf16 slices
+        OzConfig c2 = cfg;
+        c2.carrier = 1;
+        return make_plan_uncached(M, N, K, c2, out, err, bin_lo, bin_hi, hints);
+    }
     if (!p.fn) {
         *err = "no kernel variant for this tile / accumulator / K chunk";
         return false;
@@ -443,13 +462,15 @@ bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std
     p.tiles_n = (N + p.BN - 1) / p.BN;
     p.Mp = p.tiles_m * BM;
     p.Np = p.tiles_n * p.BN;
-    p.b_slice_bytes = static_cast<uint32_t>(p.BN) * p.KC * 2;
-    p.a_block_bytes = static_cast<uint32_t>(s) * BM * p.KC * 2;
+    p.b_slice_bytes = static_cast<uint32_t>(p.BN * p.KC * eb);
+    p.a_block_bytes = static_cast<uint32_t>(s * BM * p.KC * eb);
     p.b_block_bytes = static_cast<uint32_t>(s) * p.b_slice_bytes;
     p.b_region_bytes = static_cast<uint32_t>(p.pad_lo + s + p.pad_hi) * p.b_slice_bytes;
     p.stage_bytes = p.a_block_bytes + p.b_region_bytes;
     p.a_elems = static_cast<size_t>(p.tiles_m) * p.n_kc * s * BM * p.KC;
     p.b_elems = static_cast<size_t>(p.tiles_n) * p.n_kc * s * p.BN * p.KC;
+    p.a_bytes = p.a_elems * eb;
+    p.b_bytes = p.b_elems * eb;
     uint32_t cols = 32;
     while (cols < static_cast<uint32_t>(J * p.BN)) cols <<= 1;
     p.tmem_cols = cols;
@@ -464,7 +485,9 @@ std::vector<PlanHints> plan_candidates(int M, int N, int K, const OzConfig &cfg,
     std::vector<PlanHints> out;
     std::vector<Plan> plans;
     auto same = [](const Plan &x, const Plan &y) {
-        if (x.BN != y.BN || x.KC != y.KC || x.G != y.G || x.stages != y.stages || x.n_iss != y.n_iss) return false;
+        if (x.f8 != y.f8 || x.BN != y.BN || x.KC != y.KC || x.G != y.G || x.stages != y.stages ||
+            x.n_iss != y.n_iss)
+            return false;
         for (int i = 0; i < x.G; ++i)
             if (x.blk_lo[i] != y.blk_lo[i] || x.blk_nb[i] != y.blk_nb[i]) return false;
         return true;
@@ -497,7 +520,7 @@ std::vector<PlanHints> plan_candidates(int M, int N, int K, const OzConfig &cfg,
     };
     try_add(PlanHints{});  // the cost-model choice
     const int bns[] = {128, 64, 48, 32, 16};
-    const int kcs[] = {32, 16};
+    const int kcs[] = {64, 32, 16};  // K values per chunk (64 only for e4m3 slices)
     // explicit two-block splits of the bins first (they trade UMMA width for
     // drain overlap, which the cost model does not see), then the cost model's
     // best partition for each block count

@@ -15,11 +15,14 @@ struct OzConfig {
     int s = 8;         // slices
     int J = 8;         // bins: pair set {p + q <= J - 1}
     int rounding = 0;  // OUT_RN or OUT_RZ_REF
+    int carrier = 0;   // 0: e4m3 slices where exact (b <= 4), else bf16; 1: bf16 (planes read back as bf16)
 };
 
 struct Plan {
     OzConfig cfg;
-    int BN = 0, W = 0, KC = 0, stages = 0, G = 0, min_period = 0;
+    int BN = 0, W = 0, KC = 0, stages = 0, G = 0, min_period = 0;  // KC: K values per chunk
+    bool f8 = false;                  // e4m3 slices (kind::f8f6f4) instead of bf16
+    size_t a_bytes = 0, b_bytes = 0;  // bytes of the slice blocks in HBM
     int n_kc = 0, Kp = 0, Mp = 0, Np = 0, tiles_m = 0, tiles_n = 0;
     int pairs = 0, max_pairs = 0, mma_per_kstep = 0;
     int pad_lo = 0, pad_hi = 0;

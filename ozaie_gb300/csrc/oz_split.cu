@@ -131,6 +131,28 @@ __device__ __forceinline__ uint32_t slice_bits(const uint32_t (&w)[5], uint32_t 
     return mag | (v ? sign : 0u);
 }
 
+// Four slices p of four elements as e4m3 bytes (element 0 in the lowest byte):
+// every magnitude is < 16, so the conversion is exact.
+template <int B>
+__device__ __forceinline__ float slice_float(const uint32_t (&w)[5], uint32_t sign, int p) {
+    const int pos = B * p;
+    const int idx = pos >> 5, off = pos & 31;
+    const uint32_t v = __funnelshift_l(w[idx + 1], w[idx], off) >> (32 - B);
+    const float f = __uint_as_float(0x4B000000u | v) - 8388608.0f;
+    return sign ? -f : f;
+}
+template <int B>
+__device__ __forceinline__ uint32_t slices_e4m3x4(const uint32_t (*w)[5], const uint32_t *sg, int p) {
+    uint16_t lo, hi;
+    asm("cvt.rn.satfinite.e4m3x2.f32 %0, %1, %2;"
+        : "=h"(lo)
+        : "f"(slice_float<B>(w[1], sg[1], p)), "f"(slice_float<B>(w[0], sg[0], p)));
+    asm("cvt.rn.satfinite.e4m3x2.f32 %0, %1, %2;"
+        : "=h"(hi)
+        : "f"(slice_float<B>(w[3], sg[3], p)), "f"(slice_float<B>(w[2], sg[2], p)));
+    return static_cast<uint32_t>(lo) | (static_cast<uint32_t>(hi) << 16);
+}
+
 __host__ __device__ inline bool split_two_windows(int b, int s) {
     const int avoid = 1 + (b == 3 ? 3 : 0);
     const int nv0 = 64 - avoid - ((64 - avoid) % b);
@@ -140,7 +162,7 @@ __host__ __device__ inline bool split_two_windows(int b, int s) {
 // A [M][K] row-major -> A slice blocks [mt][c][p][128 x KC].  One thread takes 8
 // consecutive K values of one row and writes one 16-byte piece per slice; a warp
 // covers 8 rows x 32 K (4 core matrices of each slice, 512 contiguous bytes).
-template <int B>
+template <int B, bool F8 = false>
 __device__ __forceinline__ void split_a_body(const double *__restrict__ A, long lda, int M, int K,
                                              const int32_t *__restrict__ er, int s, int KC, int n_kc, int Mp,
                                              uint16_t *__restrict__ tiles, int bx, int by, bool trans) {
@@ -162,6 +184,21 @@ __device__ __forceinline__ void split_a_body(const double *__restrict__ A, long 
     }
     const int mt = m >> 7, r = m & 127, c = k0 / KC, kk = k0 % KC;
     const size_t slice_elems = static_cast<size_t>(BM) * KC;
+    if constexpr (F8) {
+        // one-byte slices: 8 bytes per thread and slice
+        uint8_t *dst8 = reinterpret_cast<uint8_t *>(tiles) + (static_cast<size_t>(mt) * n_kc + c) * s * slice_elems +
+                        canon_offset8(r, kk, KC);
+#pragma unroll
+        for (int p = 0; p < 128 / B; ++p) {
+            if (p < s) {
+                uint2 v;
+                v.x = slices_e4m3x4<B>(w, sg, p);
+                v.y = slices_e4m3x4<B>(w + 4, sg + 4, p);
+                *reinterpret_cast<uint2 *>(dst8 + p * slice_elems) = v;
+            }
+        }
+        return;
+    }
     uint16_t *dst = tiles + (static_cast<size_t>(mt) * n_kc + c) * s * slice_elems + canon_offset(r, kk, KC);
 #pragma unroll
     for (int p = 0; p < 128 / B; ++p) {
@@ -175,16 +212,16 @@ __device__ __forceinline__ void split_a_body(const double *__restrict__ A, long 
         }
     }
 }
-template <int B>
+template <int B, bool F8>
 __global__ void k_split_a(const double *__restrict__ A, long lda, int M, int K, const int32_t *__restrict__ er,
                           int s, int KC, int n_kc, int Mp, uint16_t *__restrict__ tiles, int trans) {
-    split_a_body<B>(A, lda, M, K, er, s, KC, n_kc, Mp, tiles, blockIdx.x, blockIdx.y, trans != 0);
+    split_a_body<B, F8>(A, lda, M, K, er, s, KC, n_kc, Mp, tiles, blockIdx.x, blockIdx.y, trans != 0);
 }
 
 // B [K][N] row-major -> slice blocks of B^T [nt][c][q][BN x KC].  One thread
 // takes one column n and 8 consecutive K; a warp reads 32 consecutive columns
 // per row (coalesced) and writes four 128-byte core matrices per slice.
-template <int B>
+template <int B, bool F8 = false>
 __device__ __forceinline__ void split_b_body(const double *__restrict__ Bm, long ldb, int K, int N,
                                              const int32_t *__restrict__ ec, int s, int KC, int n_kc, int BN, int Np,
                                              uint16_t *__restrict__ tiles, int bx, int by, bool trans) {
@@ -205,6 +242,20 @@ __device__ __forceinline__ void split_b_body(const double *__restrict__ Bm, long
     }
     const int nt = n / BN, r = n % BN, c = k0 / KC, kk = k0 % KC;
     const size_t slice_elems = static_cast<size_t>(BN) * KC;
+    if constexpr (F8) {
+        uint8_t *dst8 = reinterpret_cast<uint8_t *>(tiles) + (static_cast<size_t>(nt) * n_kc + c) * s * slice_elems +
+                        canon_offset8(r, kk, KC);
+#pragma unroll
+        for (int q = 0; q < 128 / B; ++q) {
+            if (q < s) {
+                uint2 v;
+                v.x = slices_e4m3x4<B>(w, sg, q);
+                v.y = slices_e4m3x4<B>(w + 4, sg + 4, q);
+                *reinterpret_cast<uint2 *>(dst8 + q * slice_elems) = v;
+            }
+        }
+        return;
+    }
     uint16_t *dst = tiles + (static_cast<size_t>(nt) * n_kc + c) * s * slice_elems + canon_offset(r, kk, KC);
 #pragma unroll
     for (int q = 0; q < 128 / B; ++q) {
@@ -218,10 +269,10 @@ __device__ __forceinline__ void split_b_body(const double *__restrict__ Bm, long
         }
     }
 }
-template <int B>
+template <int B, bool F8>
 __global__ void k_split_b(const double *__restrict__ Bm, long ldb, int K, int N, const int32_t *__restrict__ ec,
                           int s, int KC, int n_kc, int BN, int Np, uint16_t *__restrict__ tiles, int trans) {
-    split_b_body<B>(Bm, ldb, K, N, ec, s, KC, n_kc, BN, Np, tiles, blockIdx.x, blockIdx.y, trans != 0);
+    split_b_body<B, F8>(Bm, ldb, K, N, ec, s, KC, n_kc, BN, Np, tiles, blockIdx.x, blockIdx.y, trans != 0);
 }
 
 // b (1..7) as a template argument: the slice positions become constants.
@@ -234,6 +285,14 @@ __global__ void k_split_b(const double *__restrict__ Bm, long ldb, int K, int N,
         case 5: CALL(5); break;    \
         case 6: CALL(6); break;    \
         default: CALL(7); break;   \
+    }
+// b <= 4 (the e4m3 carrier holds |v| <= 15 exactly)
+#define OZ_SPLIT_DISPATCH_F8(b, CALL) \
+    switch (b) {                      \
+        case 1: CALL(1); break;       \
+        case 2: CALL(2); break;       \
+        case 3: CALL(3); break;       \
+        default: CALL(4); break;      \
     }
 
 // A kernel whose only wait is on an mbarrier that nothing arrives on: exercises
@@ -566,15 +625,29 @@ __global__ void __launch_bounds__(kStageThreads) k_stage_jobs(const StageJob *__
         case JOB_STATS: stats2d_body(j.X, j.ld, j.rows, j.cols, j.e_out, j.e_out2, j.prow, j.pcol, bx, by); break;
         case JOB_SPLIT_A: {
 #define OZ_JOB_A(BB) split_a_body<BB>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.padded, j.tiles, bx, by, false)
-            OZ_SPLIT_DISPATCH(j.b, OZ_JOB_A)
+#define OZ_JOB_A8(BB) \
+    split_a_body<BB, true>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.padded, j.tiles, bx, by, false)
+            if (j.f8) {
+                OZ_SPLIT_DISPATCH_F8(j.b, OZ_JOB_A8)
+            } else {
+                OZ_SPLIT_DISPATCH(j.b, OZ_JOB_A)
+            }
 #undef OZ_JOB_A
+#undef OZ_JOB_A8
             break;
         }
         default: {
 #define OZ_JOB_B(BB) \
     split_b_body<BB>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.BN, j.padded, j.tiles, bx, by, false)
-            OZ_SPLIT_DISPATCH(j.b, OZ_JOB_B)
+#define OZ_JOB_B8(BB) \
+    split_b_body<BB, true>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.BN, j.padded, j.tiles, bx, by, false)
+            if (j.f8) {
+                OZ_SPLIT_DISPATCH_F8(j.b, OZ_JOB_B8)
+            } else {
+                OZ_SPLIT_DISPATCH(j.b, OZ_JOB_B)
+            }
 #undef OZ_JOB_B
+#undef OZ_JOB_B8
             break;
         }
     }
@@ -667,25 +740,37 @@ void launch_colmax(const double *B, long ldb, int K, int N, int32_t *ec, double 
 }
 
 void launch_split_a(const double *A, long lda, int M, int K, const int32_t *er, int b, int s, int KC, int n_kc,
-                    int Mp, uint16_t *tiles, void *stream, bool trans) {
+                    int Mp, uint16_t *tiles, void *stream, bool trans, bool f8) {
     const int Kp = n_kc * KC;
     dim3 grid((Kp / 8 + 31) / 32, Mp / 8);
-#define OZ_CALL_A(BB)                                                                                  \
-    k_split_a<BB><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(A, lda, M, K, er, s, KC, n_kc, Mp, tiles, \
-                                                                        trans ? 1 : 0)
-    OZ_SPLIT_DISPATCH(b, OZ_CALL_A)
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+#define OZ_CALL_A(BB) k_split_a<BB, false><<<grid, 256, 0, st>>>(A, lda, M, K, er, s, KC, n_kc, Mp, tiles, trans ? 1 : 0)
+#define OZ_CALL_A8(BB) k_split_a<BB, true><<<grid, 256, 0, st>>>(A, lda, M, K, er, s, KC, n_kc, Mp, tiles, trans ? 1 : 0)
+    if (f8) {
+        OZ_SPLIT_DISPATCH_F8(b, OZ_CALL_A8)
+    } else {
+        OZ_SPLIT_DISPATCH(b, OZ_CALL_A)
+    }
 #undef OZ_CALL_A
+#undef OZ_CALL_A8
 }
 
 void launch_split_b(const double *B, long ldb, int K, int N, const int32_t *ec, int b, int s, int KC, int n_kc,
-                    int BN, int Np, uint16_t *tiles, void *stream, bool trans) {
+                    int BN, int Np, uint16_t *tiles, void *stream, bool trans, bool f8) {
     const int Kp = n_kc * KC;
     dim3 grid((Np + 31) / 32, (Kp / 8 + 7) / 8);
-#define OZ_CALL_B(BB)                                                                                    \
-    k_split_b<BB><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(B, ldb, K, N, ec, s, KC, n_kc, BN, Np, tiles, \
-                                                                        trans ? 1 : 0)
-    OZ_SPLIT_DISPATCH(b, OZ_CALL_B)
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+#define OZ_CALL_B(BB) \
+    k_split_b<BB, false><<<grid, 256, 0, st>>>(B, ldb, K, N, ec, s, KC, n_kc, BN, Np, tiles, trans ? 1 : 0)
+#define OZ_CALL_B8(BB) \
+    k_split_b<BB, true><<<grid, 256, 0, st>>>(B, ldb, K, N, ec, s, KC, n_kc, BN, Np, tiles, trans ? 1 : 0)
+    if (f8) {
+        OZ_SPLIT_DISPATCH_F8(b, OZ_CALL_B8)
+    } else {
+        OZ_SPLIT_DISPATCH(b, OZ_CALL_B)
+    }
 #undef OZ_CALL_B
+#undef OZ_CALL_B8
 }
 
 int launch_selftest_timeout(int *err, unsigned long long timeout_ns, void *stream) {

@@ -226,3 +226,26 @@ def test_reference_device_output_pairs(gpu_handle, oracle, mode, shape):
     want = oracle.sum_upshift(bins, er, ec, K, b, d)
     assert np.array_equal(pairs, want)
     assert np.array_equal(oracle.decode_pairs(pairs, K, d, b).view(np.uint64), C.view(np.uint64))
+
+
+@pytest.mark.parametrize("b,s,J", [(4, 10, 10), (3, 18, 18), (4, 8, 15), (2, 12, 12)])
+def test_e4m3_carrier_bit_exact(gpu_handle, oracle, b, s, J):
+    """Slices of b <= 4 bits run on e4m3 (kind::f8f6f4, 64 K values per chunk): the
+    result keeps the oracle's bits, through several drains and the K-split."""
+    import torch
+    M, N, K = 300, 200, 3000
+    A = oracle.gen_phi((M, K), 95, 1.0)
+    B = oracle.gen_phi((K, N), 96, 1.0)
+    dev = torch.device("cuda", 0)
+    dA, dB = torch.from_numpy(A).to(dev), torch.from_numpy(B).to(dev)
+    dC = torch.full((M, N), float("nan"), dtype=torch.float64, device=dev)
+    gpu_handle.set_bits(b)
+    gpu_handle.set_slices(s)
+    gpu_handle.set_bins(J)
+    assert gpu_handle.dgemm_device(M, N, K, dA.data_ptr(), K, dB.data_ptr(), N, dC.data_ptr(), N,
+                                   torch.cuda.current_stream().cuda_stream) == 0, gpu_handle.last_error()
+    assert gpu_handle.sync() == 0, gpu_handle.last_error()
+    cfg = gpu_handle.config()
+    assert cfg["slice_format"] == 1
+    ref = oracle.dgemm(A, B, b, s, J, 0)
+    assert np.array_equal(dC.cpu().numpy().view(np.uint64), ref.view(np.uint64))
