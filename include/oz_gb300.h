@@ -159,6 +159,9 @@ ozgb_status ozgb_set_bits(ozgb_handle h, int bits);        /* 0 = profile defaul
 ozgb_status ozgb_set_slices(ozgb_handle h, int slices);    /* 0 = profile default */
 ozgb_status ozgb_set_bins(ozgb_handle h, int bins);        /* 0 = default, -1 = full pair set, else J */
 ozgb_status ozgb_set_rounding(ozgb_handle h, int rounding);
+/* Slice format: 0 = e4m3 where it is exact (b <= 4) and a kernel fits, else bf16
+ * (default); 1 = bf16 always. */
+ozgb_status ozgb_set_slice_format(ozgb_handle h, int format);
 /* Requested normwise relative error (> 0 enables slice selection from the
  * exponent spread measured by stage (a)); 0 disables it. */
 ozgb_status ozgb_set_error_bound(ozgb_handle h, double bound);

@@ -77,6 +77,7 @@ SIGNATURES = [
     ("ozgb_set_slices", _i, [_h, _i]),
     ("ozgb_set_bins", _i, [_h, _i]),
     ("ozgb_set_rounding", _i, [_h, _i]),
+    ("ozgb_set_slice_format", _i, [_h, _i]),
     ("ozgb_set_error_bound", _i, [_h, _dbl]),
     ("ozgb_set_graph", _i, [_h, _i]),
     ("ozgb_set_timeout_ms", _i, [_h, _dbl]),

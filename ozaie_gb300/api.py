@@ -134,6 +134,10 @@ class Handle:
     def set_rounding(self, r):
         return self._check(self._L.ozgb_set_rounding(self._h, int(r)))
 
+    def set_slice_format(self, fmt):
+        """0: e4m3 slices where exact (b <= 4), else bf16; 1: bf16 always."""
+        return self._check(self._L.ozgb_set_slice_format(self._h, int(fmt)))
+
     def set_error_bound(self, e):
         return self._check(self._L.ozgb_set_error_bound(self._h, float(e)))
 

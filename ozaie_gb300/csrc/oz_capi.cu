@@ -58,7 +58,7 @@ struct ozgb_context {
     int M = 0, N = 0, K = 0, mode = OZGB_MODE_FAST;
     // options
     int profile = OZGB_PROFILE_GB300;
-    int opt_bits = 0, opt_slices = 0, opt_bins = 0, opt_rounding = OZGB_ROUND_DEFAULT;
+    int opt_bits = 0, opt_slices = 0, opt_bins = 0, opt_rounding = OZGB_ROUND_DEFAULT, opt_format = 0;
     double err_bound = 0.0;
     int use_graph = 0;
     unsigned long long timeout_ns = 2000000000ull;
@@ -163,6 +163,7 @@ OzConfig resolve_config(ozgb_handle h, int K, int mode) {
     if (h->opt_bins == -1) c.J = 2 * c.s - 1;
     else if (h->opt_bins > 0) c.J = h->opt_bins;
     if (h->opt_rounding >= 0) c.rounding = h->opt_rounding;
+    c.carrier = h->opt_format;
     return c;
 }
 
@@ -1112,6 +1113,12 @@ ozgb_status ozgb_set_rounding(ozgb_handle h, int rounding) {
     if (!h || rounding < -1 || rounding > 1) return OZGB_ERR_ARG;
     std::lock_guard<std::mutex> lk(h->mu);
     h->opt_rounding = rounding;
+    return OZGB_OK;
+}
+ozgb_status ozgb_set_slice_format(ozgb_handle h, int format) {
+    if (!h || format < 0 || format > 1) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->opt_format = format;
     return OZGB_OK;
 }
 ozgb_status ozgb_set_error_bound(ozgb_handle h, double bound) {

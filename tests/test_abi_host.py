@@ -76,6 +76,7 @@ def test_option_validation(ozlib):
     assert L.ozgb_set_bits(h.raw, 8) == 7 and L.ozgb_set_bits(h.raw, 7) == 0
     assert L.ozgb_set_bins(h.raw, -2) == 7 and L.ozgb_set_bins(h.raw, -1) == 0
     assert L.ozgb_set_rounding(h.raw, 2) == 7 and L.ozgb_set_rounding(h.raw, 1) == 0
+    assert L.ozgb_set_slice_format(h.raw, 2) == 7 and L.ozgb_set_slice_format(h.raw, 1) == 0
     assert L.ozgb_set_error_bound(h.raw, -1.0) == 7 and L.ozgb_set_error_bound(h.raw, 1e-15) == 0
     assert L.ozgb_set_profile(h.raw, 2) == 7 and L.ozgb_set_profile(h.raw, 1) == 0
     assert L.ozgb_set_timeout_ms(h.raw, 0.0) == 7
