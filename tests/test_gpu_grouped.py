@@ -89,3 +89,23 @@ def test_grouped_rejects_bad_problem(gpu_handle):
     rc, _ = gpu_handle.dgemm_grouped([{"M": 0, "N": 4, "K": 4, "A": 16, "lda": 4, "B": 16, "ldb": 4, "C": 16,
                                        "ldc": 4}])
     assert rc == 1
+
+
+def test_grouped_e4m3_slices_match_single_problem_path(gpu_handle, oracle, ozlib):
+    """With 4-bit slices the grouped call's split jobs write e4m3 slices: every
+    problem keeps the bits of the single-problem path (and of the oracle)."""
+    import torch
+    rng = np.random.default_rng(17)
+    probs, host = _problems(oracle, rng, 9, [0.0])
+    gpu_handle.set_bits(4)
+    gpu_handle.set_slices(12)
+    gpu_handle.set_bins(12)
+    stream = torch.cuda.current_stream().cuda_stream
+    rc, used = gpu_handle.dgemm_grouped(probs, stream)
+    assert rc == 0, gpu_handle.last_error()
+    assert gpu_handle.sync() == 0, gpu_handle.last_error()
+    assert gpu_handle.config()["slice_format"] == 1
+    torch.cuda.synchronize()
+    for (A, B, dA, dB, dC, bound), p in zip(host, probs):
+        ref = oracle.dgemm(A, B, 4, 12, 12, 0)
+        assert np.array_equal(dC.cpu().numpy().view(np.uint64), ref.view(np.uint64)), (p["M"], p["N"], p["K"])
