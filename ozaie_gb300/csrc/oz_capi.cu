@@ -1004,6 +1004,8 @@ ozgb_status ozgb_dgemm(ozgb_handle h, int M, int N, int K, const double *A, cons
         return cuda_fail(h, e, "copy B");
     Operands o{M, N, K, static_cast<double *>(h->a.p), K, static_cast<double *>(h->b.p), N,
                static_cast<double *>(h->c.p), N};
+    // (Storing C into host memory straight from the epilogue, which the device can
+    // do over NVLink-C2C, measured slower than the copy at 1024^3 to 4096^3.)
     HostOut ho{C, false};
     if ((rc = enqueue_dgemm(h, o, h->mode, st, -1, 0, kMaxBins, nullptr, &ho))) {
         cudaStreamSynchronize(st);

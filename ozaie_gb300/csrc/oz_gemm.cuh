@@ -729,16 +729,31 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                 } else {
                     double *crow = tr.c + static_cast<size_t>(row) * tr.ldc;
                     const bool plain = g.alpha == 1.0 && g.beta == 0.0;
+                    // pairs of columns as one 16-byte store where aligned (fewer, larger
+                    // writes, which matters most when C is host memory)
+                    const bool vec = (reinterpret_cast<uintptr_t>(crow + col0) & 15) == 0;
 #pragma unroll
-                    for (int i = 0; i < COLS; ++i) {
+                    for (int i = 0; i < COLS; i += 2) {
+                        double v[2];
+#pragma unroll
+                        for (int u = 0; u < 2; ++u) {
+                            const int col = col0 + i + u;
+                            v[u] = 0.0;
+                            if (col < tr.N) {
+                                uint32_t q[W];
+                                exact_q(i + u, q);
+                                v[u] = q_to_double<W>(q, er + tr.ec[col], bJ1, g.out_mode);
+                                // BLAS semantics: C is not read when beta == 0
+                                if (!plain)
+                                    v[u] = g.beta == 0.0 ? g.alpha * v[u] : fma(g.beta, crow[col], g.alpha * v[u]);
+                            }
+                        }
                         const int col = col0 + i;
-                        if (col < tr.N) {
-                            uint32_t q[W];
-                            exact_q(i, q);
-                            double v = q_to_double<W>(q, er + tr.ec[col], bJ1, g.out_mode);
-                            // BLAS semantics: C is not read when beta == 0
-                            if (!plain) v = g.beta == 0.0 ? g.alpha * v : fma(g.beta, crow[col], g.alpha * v);
-                            crow[col] = v;
+                        if (vec && col + 1 < tr.N) {
+                            *reinterpret_cast<double2 *>(crow + col) = make_double2(v[0], v[1]);
+                        } else {
+                            if (col < tr.N) crow[col] = v[0];
+                            if (col + 1 < tr.N) crow[col + 1] = v[1];
                         }
                     }
                 }
