@@ -8,10 +8,14 @@
 //   int128 -> double reconstruction                include/oz_aie.h:92-150
 //
 // GB300 design (persistent CTAs, one per SM, each looping over 128 x BN tiles of
-// C; 576 threads: producer warp, MMA-issuer warp, 16 drain/epilogue warps):
+// C; 608 threads: producer warp, MMA-issuer warp, 16 drain/epilogue warps, and a
+// second MMA-issuer warp that takes half of the bin blocks when the plan says so):
 //   * Carrier: tcgen05.mma kind::f16 with bf16 slices (|v| <= 127 is exact in
 //     bf16) and fp32 accumulators in TMEM.  (kind::i8 is not accepted by ptxas
-//     for sm_103a.)  Every partial sum is an integer of magnitude <= 2^24 as
+//     for sm_103a.)  Slices of b <= 4 bits may instead be e4m3 (kind::f8f6f4,
+//     template F8): a 64-deep e4m3 chunk has the byte layout of a 32-deep bf16
+//     one, so only the instruction and its operand formats change.  Every
+//     partial sum is an integer of magnitude <= 2^24 as
 //     long as bin j accumulates at most KB_j K-values between drains,
 //     pairs_in_bin(j) * KB_j * (2^b-1)^2 <= 2^24, so the fp32 accumulation is exact.
 //   * TMEM holds one fp32 accumulator of BN columns per bin j (column j*BN).
@@ -34,8 +38,11 @@
 //     32 x 32 -> 64-bit multiply-add by 2^rel into the 64-bit accumulator of the
 //     bin's group (consecutive bins whose weights relative to the group's first
 //     bin stay <= 2^30).  The W-word exact sum is assembled once per element in
-//     the epilogue.  Integer ALU work competes with the single MMA-issuing
-//     thread, so the drain keeps it to two instructions per value.
+//     the epilogue.  Integer ALU work competes with the MMA-issuing thread on its
+//     scheduler, so the drain keeps it to two instructions per value.
+//   * The last partial wave of a launch may be split along K (split_parts): the
+//     parts add their 64-bit group sums into global scratch with atomics and
+//     the part that completes a tile's count rounds and stores it.
 //   * Epilogue: the exact accumulator q is rounded once to FP64 with the scale
 //     2^{Er+Ec-2044-b(J+1)} (round-to-nearest, or the reference's truncating
 //     decode, or written raw for parity dumps).
@@ -444,8 +451,8 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
             constexpr uint32_t sbo = KC * 16;
             constexpr int ksteps = KC >> 4;
             {
-                // per-block UMMA parameters, once: with a single issuing thread every
-                // scalar instruction between UMMAs leaves the tensor core idle
+                // per-block UMMA parameters, once: every scalar instruction of the issuing
+                // thread between UMMAs can leave the tensor core idle
                 const uint32_t a0 = smem_u32(smem);
                 const uint64_t ad0 = smem_desc(a0, 128, sbo);
                 const uint64_t bd0 = smem_desc(a0 + g.a_block_bytes + g.b_pad_lo_bytes, 128, sbo);
