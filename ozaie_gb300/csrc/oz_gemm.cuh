@@ -692,7 +692,12 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
             const int row = tr.mt * BM + 32 * qd + lane;
             const int col0 = tr.nt * BN + part * COLS;
             if (row < tr.M) {
-                const int er = tr.er[row];
+                // the scale exponents first, as independent loads, so that their
+                // latency is paid once rather than once per column
+                const int er = __ldg(tr.er + row);
+                int es[COLS];
+#pragma unroll
+                for (int i = 0; i < COLS; ++i) es[i] = er + (col0 + i < tr.N ? __ldg(tr.ec + col0 + i) : 0);
                 const int bJ1 = g.b * (g.J + 1);
                 // the exact sum of column i: sum_a acc[i][a] 2^(b acc_t0[a]) in W words
                 auto exact_q = [&](int i, uint32_t (&q)[W]) {
@@ -714,7 +719,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                             unsigned long long hi = 0;
                             if constexpr (NA > 1) hi = g.n_acc > 1 ? static_cast<unsigned long long>(acc[i][1]) : 0ull;
                             const unsigned long long scale =
-                                static_cast<unsigned long long>(static_cast<uint32_t>(er + tr.ec[col]));
+                                static_cast<unsigned long long>(static_cast<uint32_t>(es[i]));
                             hi = (hi & 0x8007FFFFFFFFFFFFull) | ((scale & 0xFFFull) << 51);
                             dst[0] = static_cast<long long>(lo);
                             dst[1] = static_cast<long long>(hi);
@@ -749,7 +754,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                             if (col < tr.N) {
                                 uint32_t q[W];
                                 exact_q(i + u, q);
-                                v[u] = q_to_double<W>(q, er + tr.ec[col], bJ1, g.out_mode);
+                                v[u] = q_to_double<W>(q, es[i + u], bJ1, g.out_mode);
                                 // BLAS semantics: C is not read when beta == 0
                                 if (!plain)
                                     v[u] = g.beta == 0.0 ? g.alpha * v[u] : fma(g.beta, crow[col], g.alpha * v[u]);
