@@ -252,20 +252,33 @@ ozgb_status enqueue_exponents(ozgb_handle h, const Operands &o, bool want_ss, cu
         unsigned long long *pa = static_cast<unsigned long long *>(h->kpart.p), *pb = pa + na;
         cudaMemsetAsync(er, 0, sizeof(int32_t) * o.M, st);
         const StatsLayout la = stats_layout(ar, ac), lb = stats_layout(br, bc);
-        launch_stats2d(o.A, o.lda, ar, ac, o.ta ? nullptr : er, o.ta ? er : nullptr, pa, pa + la.row_n, st);
-        launch_stats2d(o.B, o.ldb, br, bc, o.tb ? ec : nullptr, o.tb ? nullptr : ec, pb, pb + lb.row_n, st);
+        // both operands' fused passes in one launch
+        StageJob ja{}, jb{};
+        ja.kind = JOB_STATS, ja.X = o.A, ja.ld = o.lda, ja.rows = ar, ja.cols = ac;
+        ja.e_out = o.ta ? nullptr : er, ja.e_out2 = o.ta ? er : nullptr, ja.prow = pa, ja.pcol = pa + la.row_n;
+        jb.kind = JOB_STATS, jb.X = o.B, jb.ld = o.ldb, jb.rows = br, jb.cols = bc;
+        jb.e_out = o.tb ? ec : nullptr, jb.e_out2 = o.tb ? nullptr : ec, jb.prow = pb, jb.pcol = pb + lb.row_n;
+        launch_stage_pair(ja, jb, st);
         h->kjob = knob_job(o, er, ec, pa, pb);
-    } else if (o.ta) {
-        cudaMemsetAsync(er, 0, sizeof(int32_t) * o.M, st);
-        launch_colmax(o.A, o.lda, o.K, o.M, er, nullptr, st);  // rows of op(A) are columns of A
     } else {
-        launch_rowmax(o.A, o.lda, o.M, o.K, er, nullptr, st);
+        // exponent maxima of the rows of op(A) and the columns of op(B), one launch
+        StageJob ja{}, jb{};
+        if (o.ta) {  // rows of op(A) are columns of A
+            cudaMemsetAsync(er, 0, sizeof(int32_t) * o.M, st);
+            ja.kind = JOB_COLMAX, ja.rows = o.K, ja.cols = o.M;
+        } else {
+            ja.kind = JOB_ROWMAX, ja.rows = o.M, ja.cols = o.K;
+        }
+        ja.X = o.A, ja.ld = o.lda, ja.e_out = er;
+        if (o.tb) {  // columns of op(B) are rows of B
+            jb.kind = JOB_ROWMAX, jb.rows = o.N, jb.cols = o.K;
+        } else {
+            jb.kind = JOB_COLMAX, jb.rows = o.K, jb.cols = o.N;
+        }
+        jb.X = o.B, jb.ld = o.ldb, jb.e_out = ec;
+        launch_stage_pair(ja, jb, st);
     }
-    if (!want_ss) {
-        if (o.tb) launch_rowmax(o.B, o.ldb, o.N, o.K, ec, nullptr, st);  // columns of op(B) are rows of B
-        else launch_colmax(o.B, o.ldb, o.K, o.N, ec, nullptr, st);
-    }
-    h->launches += 2;
+    h->launches += 1;
     return OZGB_OK;
 }
 
@@ -418,11 +431,29 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
     if (!h->at.ensure(p.a_bytes) || !h->bt.ensure(p.b_bytes))
         return fail(h, OZGB_ERR_ALLOC, "slice buffers");
     uint16_t *at = static_cast<uint16_t *>(h->at.p), *bt = static_cast<uint16_t *>(h->bt.p);
-    launch_split_a(o.A, o.lda, o.M, o.K, static_cast<int32_t *>(h->er.p), p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.Mp, at, st,
-                   o.ta, p.f8);
-    launch_split_b(o.B, o.ldb, o.K, o.N, static_cast<int32_t *>(h->ec.p), p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.BN, p.Np,
-                   bt, st, o.tb, p.f8);
-    h->launches += 2;
+    // small operands: both splits in one launch (one launch gap less); large ones
+    // run the separate kernels, whose lighter register and shared-memory use
+    // measured faster (4096^3: 0.270 against 0.291 ms)
+    const double elems = static_cast<double>(p.Mp + p.Np) * p.n_kc * p.KC;
+    if (elems > 16.0 * 1024 * 1024) {
+        launch_split_a(o.A, o.lda, o.M, o.K, static_cast<int32_t *>(h->er.p), p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.Mp, at,
+                       st, o.ta, p.f8);
+        launch_split_b(o.B, o.ldb, o.K, o.N, static_cast<int32_t *>(h->ec.p), p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.BN,
+                       p.Np, bt, st, o.tb, p.f8);
+        h->launches += 2;
+    } else {
+        StageJob ja{}, jb{};
+        ja.kind = JOB_SPLIT_A, ja.X = o.A, ja.ld = o.lda, ja.rows = o.M, ja.cols = o.K;
+        ja.e_in = static_cast<int32_t *>(h->er.p), ja.padded = p.Mp, ja.trans = o.ta ? 1 : 0, ja.tiles = at;
+        jb.kind = JOB_SPLIT_B, jb.X = o.B, jb.ld = o.ldb, jb.rows = o.K, jb.cols = o.N;
+        jb.e_in = static_cast<int32_t *>(h->ec.p), jb.padded = p.Np, jb.trans = o.tb ? 1 : 0, jb.tiles = bt;
+        for (StageJob *j : {&ja, &jb}) {
+            j->b = p.cfg.b, j->s = p.cfg.s, j->KC = p.KC, j->n_kc = p.n_kc, j->BN = p.BN;
+            j->f8 = p.f8 ? 1 : 0;
+        }
+        launch_stage_pair(ja, jb, st);
+        h->launches += 1;
+    }
     if (h->profiling) cudaEventRecord(h->ev[2], st);
     GemmArgs g;
     gemm_args_from_plan(&g, p, out_mode, static_cast<int *>(h->err.p), h->timeout_ns);

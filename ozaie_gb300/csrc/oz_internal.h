@@ -131,6 +131,7 @@ struct StageJob {
     const int32_t *e_in; // SPLIT: row (A) / column (B) exponents
     int b, s, KC, n_kc, padded, BN;  // SPLIT: padded = Mp (A) or Np (B)
     int f8;                          // SPLIT: e4m3 slices (b <= 4)
+    int trans;                       // SPLIT: A stored K x M / B stored N x K
     uint16_t *tiles;
     int32_t *e_out2;                  // STATS: column exponent fields (atomic max, may be null)
     unsigned long long *prow, *pcol;  // STATS: row partials [rows][ceil(cols/256)], column partials [ceil(rows/64)][cols]
@@ -195,6 +196,9 @@ void stage_grid(const StageJob &j, int *gx, int *gy);
 // Grouped launches: all jobs in one grid (block0[i] = first block of job i,
 // block0[n_jobs] = total), and the knob reduction of n problems.
 void launch_stage_jobs(const StageJob *jobs, const int *block0, int n_jobs, int total_blocks, void *stream);
+// Two jobs (for example the A and B halves of one stage) in one launch; the grid
+// sizes are filled in here.
+void launch_stage_pair(StageJob j0, StageJob j1, void *stream);
 void launch_knob_grouped(const KnobJob *jobs, int n, void *stream);
 // C = beta * C (zeros for beta == 0, C not read).
 void launch_scale(double *C, long ldc, int M, int N, double beta, void *stream);

@@ -607,26 +607,18 @@ __global__ void k_knob_grouped(const KnobJob *__restrict__ jobs) {
 
 // Grouped stage (a)/(b): block -> job by binary search over block0[], then the
 // job's per-problem kernel body with its local block coordinates.
-__global__ void __launch_bounds__(kStageThreads) k_stage_jobs(const StageJob *__restrict__ jobs,
-                                                              const int *__restrict__ block0, int n_jobs) {
-    int lo = 0, hi = n_jobs - 1;
-    const int bid = blockIdx.x;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (__ldg(block0 + mid) <= bid) lo = mid;
-        else hi = mid - 1;
-    }
-    const StageJob &j = jobs[lo];
-    const int local = bid - __ldg(block0 + lo);
+// One stage job on its local block index (the per-problem kernels' bodies).
+__device__ __forceinline__ void run_stage_job(const StageJob &j, int local) {
     const int bx = local % j.gx, by = local / j.gx;
+    const bool tr = j.trans != 0;
     switch (j.kind) {
         case JOB_ROWMAX: rowmax_body(j.X, j.ld, j.rows, j.cols, j.e_out, j.ss_out, bx, by); break;
         case JOB_COLMAX: colmax_body(j.X, j.ld, j.rows, j.cols, 64, j.e_out, j.ss_out, bx, by); break;
         case JOB_STATS: stats2d_body(j.X, j.ld, j.rows, j.cols, j.e_out, j.e_out2, j.prow, j.pcol, bx, by); break;
         case JOB_SPLIT_A: {
-#define OZ_JOB_A(BB) split_a_body<BB>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.padded, j.tiles, bx, by, false)
+#define OZ_JOB_A(BB) split_a_body<BB>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.padded, j.tiles, bx, by, tr)
 #define OZ_JOB_A8(BB) \
-    split_a_body<BB, true>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.padded, j.tiles, bx, by, false)
+    split_a_body<BB, true>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.padded, j.tiles, bx, by, tr)
             if (j.f8) {
                 OZ_SPLIT_DISPATCH_F8(j.b, OZ_JOB_A8)
             } else {
@@ -638,9 +630,9 @@ __global__ void __launch_bounds__(kStageThreads) k_stage_jobs(const StageJob *__
         }
         default: {
 #define OZ_JOB_B(BB) \
-    split_b_body<BB>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.BN, j.padded, j.tiles, bx, by, false)
+    split_b_body<BB>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.BN, j.padded, j.tiles, bx, by, tr)
 #define OZ_JOB_B8(BB) \
-    split_b_body<BB, true>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.BN, j.padded, j.tiles, bx, by, false)
+    split_b_body<BB, true>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.BN, j.padded, j.tiles, bx, by, tr)
             if (j.f8) {
                 OZ_SPLIT_DISPATCH_F8(j.b, OZ_JOB_B8)
             } else {
@@ -651,6 +643,26 @@ __global__ void __launch_bounds__(kStageThreads) k_stage_jobs(const StageJob *__
             break;
         }
     }
+}
+
+__global__ void __launch_bounds__(kStageThreads) k_stage_jobs(const StageJob *__restrict__ jobs,
+                                                              const int *__restrict__ block0, int n_jobs) {
+    int lo = 0, hi = n_jobs - 1;
+    const int bid = blockIdx.x;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(block0 + mid) <= bid) lo = mid;
+        else hi = mid - 1;
+    }
+    run_stage_job(jobs[lo], bid - __ldg(block0 + lo));
+}
+
+// Two jobs of one problem (A and B) in one launch: blocks [0, n0) run j0.
+__global__ void __launch_bounds__(kStageThreads) k_stage_pair(const __grid_constant__ StageJob j0,
+                                                              const __grid_constant__ StageJob j1, int n0) {
+    const int bid = blockIdx.x;
+    if (bid < n0) run_stage_job(j0, bid);
+    else run_stage_job(j1, bid - n0);
 }
 
 // Pseudo-random doubles in [-1, 1) (splitmix64 of the index): inputs for the
@@ -708,6 +720,14 @@ void stage_grid(const StageJob &j, int *gx, int *gy) {
             *gy = (j.n_kc * j.KC / 8 + 7) / 8;
             break;
     }
+}
+
+void launch_stage_pair(StageJob j0, StageJob j1, void *stream) {
+    stage_grid(j0, &j0.gx, &j0.gy);
+    stage_grid(j1, &j1.gx, &j1.gy);
+    const int n0 = j0.gx * j0.gy, n1 = j1.gx * j1.gy;
+    if (n0 + n1 > 0)
+        k_stage_pair<<<n0 + n1, kStageThreads, 0, static_cast<cudaStream_t>(stream)>>>(j0, j1, n0);
 }
 
 void launch_stage_jobs(const StageJob *jobs, const int *block0, int n_jobs, int total_blocks, void *stream) {
