@@ -389,85 +389,83 @@ __device__ __forceinline__ void sq_add_em(int &E, float &s, int e, float m2) {
     s = fmaf(m2, pow4f(e - E), s);
 }
 
-// One 64-row x 256-column tile.  Thread t owns column bx*256+t (coalesced row
-// reads, 8 rows in flight); the rows are reduced through shared memory 8 rows
-// at a time, one warp per row.
+// One 64-row x 256-column tile.  Lane l of each warp owns the 8 columns
+// bx*256 + l + 32k (each load instruction of a warp reads 256 contiguous bytes)
+// and warp w the rows w, w+8, ..., so a row is reduced by the
+// warp's shuffles alone (no block barrier in the row loop); the 8 warps' column
+// partials are merged once through shared memory at the end.
 __device__ __forceinline__ void stats2d_body(const double *__restrict__ X, long ld, int rows, int cols,
                                              int32_t *__restrict__ row_e, int32_t *__restrict__ col_e,
                                              unsigned long long *__restrict__ row_part,
                                              unsigned long long *__restrict__ col_part, int bx, int by) {
-    constexpr int RB = kStageThreads / 32;  // rows per chunk = warps per block
-    __shared__ int shE[RB][kStatsCols];
-    __shared__ float shM[RB][kStatsCols];
-    __shared__ int rE[kStatsRows];
-    __shared__ float rS[kStatsRows];
+    constexpr int NW = kStageThreads / 32;           // warps per block
+    constexpr int CPL = kStatsCols / 32;             // columns per lane (8)
+    static_assert(CPL == 8 && kStatsRows % NW == 0, "stats tile");
+    __shared__ int shE[NW][kStatsCols];
+    __shared__ float shS[NW][kStatsCols];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int c = bx * kStatsCols + threadIdx.x;
+    const int c0 = bx * kStatsCols + lane;            // this lane's first column; then every 32nd
     const int r0 = by * kStatsRows;
-    const bool cin = c < cols;
     const bool rows_wanted = row_e || row_part;
-    int Ec = 0;
-    float sc = 0.0f;
-    // the next chunk's rows are loaded before this chunk's reduction and barriers
-    double x[RB], xn[RB];
+    const int nbx = (cols + kStatsCols - 1) / kStatsCols;
+    int Ec[CPL];
+    float sc[CPL];
 #pragma unroll
-    for (int u = 0; u < RB; ++u) {
-        const int r = r0 + u;
-        x[u] = (cin && r < rows) ? __ldg(X + static_cast<size_t>(r) * ld + c) : 0.0;
+    for (int k = 0; k < CPL; ++k) {
+        Ec[k] = 0;
+        sc[k] = 0.0f;
     }
-    for (int i0 = 0; i0 < kStatsRows; i0 += RB) {
+    auto load_row = [&](int r, double (&x)[CPL]) {
 #pragma unroll
-        for (int u = 0; u < RB; ++u) {
-            const int r = r0 + i0 + RB + u;
-            xn[u] = (cin && i0 + RB < kStatsRows && r < rows) ? __ldg(X + static_cast<size_t>(r) * ld + c) : 0.0;
-        }
+        for (int k = 0; k < CPL; ++k)
+            x[k] = (r < rows && c0 + 32 * k < cols) ? __ldg(X + static_cast<size_t>(r) * ld + c0 + 32 * k) : 0.0;
+    };
+    double x[CPL];
+    for (int i = wid; i < kStatsRows; i += NW) {
+        const int r = r0 + i;
+        load_row(r, x);
+        int Er = 0;
+        float sr = 0.0f;
 #pragma unroll
-        for (int u = 0; u < RB; ++u) {
-            const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(x[u]));
+        for (int k = 0; k < CPL; ++k) {
+            const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(x[k]));
             const int e = static_cast<int>((bits >> 52) & 0x7FF);
             float m2 = 0.0f;
             if (e != 0 && e != 0x7FF) {
                 const float m = __uint_as_float(0x3F800000u | static_cast<uint32_t>((bits >> 29) & 0x7FFFFF));
                 m2 = m * m;
             }
-            sq_add_em(Ec, sc, e, m2);
-            if (rows_wanted) {
-                shE[u][threadIdx.x] = e;
-                shM[u][threadIdx.x] = m2;
-            }
+            sq_add_em(Ec[k], sc[k], e, m2);
+            sq_add_em(Er, sr, e, m2);
         }
         if (rows_wanted) {
-            __syncthreads();
-            int E = 0;
-            float sr = 0.0f;
-            for (int q = lane; q < kStatsCols; q += 32) sq_merge(E, sr, shE[wid][q], shM[wid][q]);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                const int e2 = __shfl_xor_sync(0xffffffffu, E, o);
+                const int e2 = __shfl_xor_sync(0xffffffffu, Er, o);
                 const float s2 = __shfl_xor_sync(0xffffffffu, sr, o);
-                sq_merge(E, sr, e2, s2);
+                sq_merge(Er, sr, e2, s2);
             }
-            if (lane == 0) {
-                rE[i0 + wid] = E;
-                rS[i0 + wid] = sr;
+            if (lane == 0 && r < rows) {
+                if (row_part) row_part[static_cast<size_t>(r) * nbx + bx] = sq_pack(Er, sr);
+                if (row_e) atomicMax(row_e + r, Er);
             }
-            __syncthreads();
         }
+    }
+    // columns: merge the warps' partials
 #pragma unroll
-        for (int u = 0; u < RB; ++u) x[u] = xn[u];
+    for (int k = 0; k < CPL; ++k) {
+        shE[wid][lane + 32 * k] = Ec[k];
+        shS[wid][lane + 32 * k] = sc[k];
     }
-    if (rows_wanted) {
-        const int r = r0 + static_cast<int>(threadIdx.x);
-        if (threadIdx.x < kStatsRows && r < rows) {
-            if (row_part)
-                row_part[static_cast<size_t>(r) * ((cols + kStatsCols - 1) / kStatsCols) + bx] =
-                    sq_pack(rE[threadIdx.x], rS[threadIdx.x]);
-            if (row_e) atomicMax(row_e + r, rE[threadIdx.x]);
-        }
-    }
-    if (cin) {
-        if (col_part) col_part[static_cast<size_t>(by) * cols + c] = sq_pack(Ec, sc);
-        if (col_e) atomicMax(col_e + c, Ec);
+    __syncthreads();
+    const int c = bx * kStatsCols + static_cast<int>(threadIdx.x);
+    if (c < cols) {
+        int E = 0;
+        float sv = 0.0f;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) sq_merge(E, sv, shE[w][threadIdx.x], shS[w][threadIdx.x]);
+        if (col_part) col_part[static_cast<size_t>(by) * cols + c] = sq_pack(E, sv);
+        if (col_e) atomicMax(col_e + c, E);
     }
 }
 
@@ -608,38 +606,76 @@ __global__ void k_knob_grouped(const KnobJob *__restrict__ jobs) {
 // Grouped stage (a)/(b): block -> job by binary search over block0[], then the
 // job's per-problem kernel body with its local block coordinates.
 // One stage job on its local block index (the per-problem kernels' bodies).
+// TRANS: the kernel also serves transposed splits (the grouped kernel does not,
+// which keeps its register count down).
+template <bool TRANS>
 __device__ __forceinline__ void run_stage_job(const StageJob &j, int local) {
     const int bx = local % j.gx, by = local / j.gx;
-    const bool tr = j.trans != 0;
+    const bool tr = TRANS && j.trans != 0;
     switch (j.kind) {
         case JOB_ROWMAX: rowmax_body(j.X, j.ld, j.rows, j.cols, j.e_out, j.ss_out, bx, by); break;
         case JOB_COLMAX: colmax_body(j.X, j.ld, j.rows, j.cols, 64, j.e_out, j.ss_out, bx, by); break;
         case JOB_STATS: stats2d_body(j.X, j.ld, j.rows, j.cols, j.e_out, j.e_out2, j.prow, j.pcol, bx, by); break;
+        // the transpose flag as a constant at each call site: a runtime flag would
+        // compile both load paths into every split (measured 20 % slower)
         case JOB_SPLIT_A: {
-#define OZ_JOB_A(BB) split_a_body<BB>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.padded, j.tiles, bx, by, tr)
-#define OZ_JOB_A8(BB) \
-    split_a_body<BB, true>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.padded, j.tiles, bx, by, tr)
+#define OZ_JOB_A(BB, T) \
+    split_a_body<BB>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.padded, j.tiles, bx, by, T)
+#define OZ_JOB_A8(BB, T) \
+    split_a_body<BB, true>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.padded, j.tiles, bx, by, T)
+#define OZ_JOB_AN(BB) OZ_JOB_A(BB, false)
+#define OZ_JOB_AT(BB) OZ_JOB_A(BB, true)
+#define OZ_JOB_A8N(BB) OZ_JOB_A8(BB, false)
+#define OZ_JOB_A8T(BB) OZ_JOB_A8(BB, true)
             if (j.f8) {
-                OZ_SPLIT_DISPATCH_F8(j.b, OZ_JOB_A8)
+                if (tr) {
+                    OZ_SPLIT_DISPATCH_F8(j.b, OZ_JOB_A8T)
+                } else {
+                    OZ_SPLIT_DISPATCH_F8(j.b, OZ_JOB_A8N)
+                }
             } else {
-                OZ_SPLIT_DISPATCH(j.b, OZ_JOB_A)
+                if (tr) {
+                    OZ_SPLIT_DISPATCH(j.b, OZ_JOB_AT)
+                } else {
+                    OZ_SPLIT_DISPATCH(j.b, OZ_JOB_AN)
+                }
             }
 #undef OZ_JOB_A
 #undef OZ_JOB_A8
+#undef OZ_JOB_AN
+#undef OZ_JOB_AT
+#undef OZ_JOB_A8N
+#undef OZ_JOB_A8T
             break;
         }
         default: {
-#define OZ_JOB_B(BB) \
-    split_b_body<BB>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.BN, j.padded, j.tiles, bx, by, tr)
-#define OZ_JOB_B8(BB) \
-    split_b_body<BB, true>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.BN, j.padded, j.tiles, bx, by, tr)
+#define OZ_JOB_B(BB, T) \
+    split_b_body<BB>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.BN, j.padded, j.tiles, bx, by, T)
+#define OZ_JOB_B8(BB, T) \
+    split_b_body<BB, true>(j.X, j.ld, j.rows, j.cols, j.e_in, j.s, j.KC, j.n_kc, j.BN, j.padded, j.tiles, bx, by, T)
+#define OZ_JOB_BN(BB) OZ_JOB_B(BB, false)
+#define OZ_JOB_BT(BB) OZ_JOB_B(BB, true)
+#define OZ_JOB_B8N(BB) OZ_JOB_B8(BB, false)
+#define OZ_JOB_B8T(BB) OZ_JOB_B8(BB, true)
             if (j.f8) {
-                OZ_SPLIT_DISPATCH_F8(j.b, OZ_JOB_B8)
+                if (tr) {
+                    OZ_SPLIT_DISPATCH_F8(j.b, OZ_JOB_B8T)
+                } else {
+                    OZ_SPLIT_DISPATCH_F8(j.b, OZ_JOB_B8N)
+                }
             } else {
-                OZ_SPLIT_DISPATCH(j.b, OZ_JOB_B)
+                if (tr) {
+                    OZ_SPLIT_DISPATCH(j.b, OZ_JOB_BT)
+                } else {
+                    OZ_SPLIT_DISPATCH(j.b, OZ_JOB_BN)
+                }
             }
 #undef OZ_JOB_B
 #undef OZ_JOB_B8
+#undef OZ_JOB_BN
+#undef OZ_JOB_BT
+#undef OZ_JOB_B8N
+#undef OZ_JOB_B8T
             break;
         }
     }
@@ -654,15 +690,15 @@ __global__ void __launch_bounds__(kStageThreads) k_stage_jobs(const StageJob *__
         if (__ldg(block0 + mid) <= bid) lo = mid;
         else hi = mid - 1;
     }
-    run_stage_job(jobs[lo], bid - __ldg(block0 + lo));
+    run_stage_job<false>(jobs[lo], bid - __ldg(block0 + lo));
 }
 
 // Two jobs of one problem (A and B) in one launch: blocks [0, n0) run j0.
 __global__ void __launch_bounds__(kStageThreads) k_stage_pair(const __grid_constant__ StageJob j0,
                                                               const __grid_constant__ StageJob j1, int n0) {
     const int bid = blockIdx.x;
-    if (bid < n0) run_stage_job(j0, bid);
-    else run_stage_job(j1, bid - n0);
+    if (bid < n0) run_stage_job<true>(j0, bid);
+    else run_stage_job<true>(j1, bid - n0);
 }
 
 // Pseudo-random doubles in [-1, 1) (splitmix64 of the index): inputs for the
