@@ -16,6 +16,12 @@
  * Every function returns an ozgb_status (0 = success).  No function falls back
  * to the CPU: without a usable CUDA device the compute entry points return
  * OZGB_ERR_NO_DEVICE.
+ *
+ * Handles: calls on one handle are serialised on the host (a mutex) and reuse
+ * the handle's device buffers (exponents, slice planes, split sums), so two
+ * calls on one handle must not overlap on the GPU: give each stream its own
+ * handle.  Buffers grow on first use (cudaMalloc); warm a handle up before
+ * capturing its calls in a CUDA graph.
  */
 #ifndef OZ_GB300_H
 #define OZ_GB300_H
