@@ -182,12 +182,6 @@ void launch_split_a(const double *A, long lda, int M, int K, const int32_t *er, 
 void launch_split_b(const double *B, long ldb, int K, int N, const int32_t *ec, int b, int s, int KC, int n_kc,
                     int BN, int Np, uint16_t *tiles, void *stream, bool trans = false, bool f8 = false);
 int launch_selftest_timeout(int *err, unsigned long long timeout_ns, void *stream);
-// One pass over a row-major rows x cols operand: exponent maxima of its rows
-// and/or columns (atomic max into row_e / col_e, zeroed before; either may be
-// null) and the partial sums of squares of its rows and columns (StatParts
-// layouts: row_part[r * ceil(cols/256) + i], col_part[i * cols + c]).
-void launch_stats2d(const double *X, long ld, int rows, int cols, int32_t *row_e, int32_t *col_e,
-                    unsigned long long *row_part, unsigned long long *col_part, void *stream);
 // Precision-knob statistics (five doubles, see KnobStats in oz_plan.h) of one
 // problem; zeroes j.out first.
 void launch_knob_stats(const KnobJob &j, void *stream);

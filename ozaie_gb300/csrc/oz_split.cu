@@ -469,18 +469,6 @@ __device__ __forceinline__ void stats2d_body(const double *__restrict__ X, long 
     }
 }
 
-__global__ void __launch_bounds__(kStageThreads) k_stats2d(const double *__restrict__ X, long ld, int rows, int cols,
-                                                           int32_t *row_e, int32_t *col_e, unsigned long long *row_part,
-                                                           unsigned long long *col_part) {
-    stats2d_body(X, ld, rows, cols, row_e, col_e, row_part, col_part, blockIdx.x, blockIdx.y);
-}
-
-void launch_stats2d(const double *X, long ld, int rows, int cols, int32_t *row_e, int32_t *col_e,
-                    unsigned long long *row_part, unsigned long long *col_part, void *stream) {
-    dim3 grid((cols + kStatsCols - 1) / kStatsCols, (rows + kStatsRows - 1) / kStatsRows);
-    k_stats2d<<<grid, kStageThreads, 0, static_cast<cudaStream_t>(stream)>>>(X, ld, rows, cols, row_e, col_e, row_part,
-                                                                              col_part);
-}
 
 // Combined (E, s) of unit u, by one warp: lanes load the unit's partials in
 // parallel and merge them; every lane returns the result.
