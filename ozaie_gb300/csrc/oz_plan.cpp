@@ -297,12 +297,12 @@ bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std
         // (about 0.1 SM cycles per value: 16 F2I conversions per cycle) before its
         // next UMMA; the other blocks' UMMAs of that chunk and the next one cover
         // the read-out, and what they do not cover stalls the tensor pipe once per
-        // drain period.  Modelled per 32-deep chunk.
+        // drain period.  Modelled per chunk.
         auto period_of = [&](int lo, int nb) {
             long kb = 1L << 40;
             for (int j = lo; j < lo + nb; ++j)
                 kb = std::min(kb, static_cast<long>(std::floor(16777216.0 / (pairs_in_bin(j, s) * v2 * v2))));
-            return std::max(1L, kb / 32);
+            return std::max(1L, kb / (p.f8 ? 64 : 32));  // chunks of 32 bf16 or 64 e4m3 K values
         };
         auto total_cost = [&](int G, const int *lo, const int *nb) {
             double umma[kMaxGroups], all = 0.0;
