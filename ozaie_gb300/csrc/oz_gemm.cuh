@@ -223,6 +223,43 @@ __device__ __forceinline__ double q_to_double(const uint32_t (&q)[W], int escale
     return __longlong_as_double(static_cast<long long>(bits));
 }
 
+// The same rounding (OUT_RN) for q = a0 + a1 2^B with 0 <= B <= 63, the exact sum
+// of at most two accumulator groups: one signed 128-bit integer, so the rounding
+// needs no word selects.  Bit for bit the result of q_to_double.
+__device__ __forceinline__ double acc2_to_double_rn(long long a0, long long a1, int B, int escale, int bJ1) {
+    const __int128 S = static_cast<__int128>(a0) + (static_cast<__int128>(a1) << B);
+    if (S == 0) return 0.0;
+    const bool neg = S < 0;
+    const unsigned __int128 m = neg ? static_cast<unsigned __int128>(-S) : static_cast<unsigned __int128>(S);
+    const unsigned long long hi = static_cast<unsigned long long>(m >> 64), lo = static_cast<unsigned long long>(m);
+    const int L = hi ? 128 - __clzll(static_cast<long long>(hi)) : 64 - __clzll(static_cast<long long>(lo));
+    const int e2 = escale - 2044 - bJ1;
+    const int biased = L - 1 + e2 + 1023;
+    const int sh = (biased >= 1) ? L - 53 : L - 53 + (1 - biased);
+    unsigned long long mm;
+    if (sh < 0) mm = (-sh >= 64) ? 0ull : (lo << (-sh));  // L < 53: m is lo
+    else mm = (sh > L) ? 0ull : static_cast<unsigned long long>(m >> sh);
+    const int rpos = sh - 1;  // the rounding bit's position
+    const int rb = (rpos < 0 || rpos >= L) ? 0 : static_cast<int>((m >> rpos) & 1u);
+    bool st = false;          // any bit below the rounding bit
+    if (rpos >= 128) st = true;  // m != 0
+    else if (rpos > 0) st = (m & ((static_cast<unsigned __int128>(1) << rpos) - 1u)) != 0;
+    if (rb && (st || (mm & 1ull))) mm++;
+    uint64_t bits;
+    if (biased >= 1) {
+        if (biased >= 2047) {
+            bits = 0x7FF0000000000000ull;
+        } else {
+            bits = (static_cast<uint64_t>(biased - 1) << 52) + mm;
+            if (bits >= 0x7FF0000000000000ull) bits = 0x7FF0000000000000ull;
+        }
+    } else {
+        bits = mm;
+    }
+    if (neg) bits |= 0x8000000000000000ull;
+    return __longlong_as_double(static_cast<long long>(bits));
+}
+
 // ------------------------------------------------------------ drain schedule
 // Block g is drained after chunk c when (c + 1 + blk_off[g]) % blk_period[g] == 0,
 // and every block after the last chunk.  The MMA issuer and the drain warps step
@@ -744,6 +781,10 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                     // pairs of columns as one 16-byte store where aligned (fewer, larger
                     // writes, which matters most when C is host memory)
                     const bool vec = (reinterpret_cast<uintptr_t>(crow + col0) & 15) == 0;
+                    // at most two accumulator groups, the second at most 63 bits up: the
+                    // 128-bit rounding path
+                    const int B1 = g.n_acc > 1 ? g.b * g.acc_t0[1] : 0;
+                    const bool two_groups = g.out_mode == OUT_RN && g.n_acc <= 2 && B1 <= 63;
 #pragma unroll
                     for (int i = 0; i < COLS; i += 2) {
                         double v[2];
@@ -752,9 +793,15 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                             const int col = col0 + i + u;
                             v[u] = 0.0;
                             if (col < tr.N) {
-                                uint32_t q[W];
-                                exact_q(i + u, q);
-                                v[u] = q_to_double<W>(q, es[i + u], bJ1, g.out_mode);
+                                if (two_groups) {
+                                    long long a1 = 0;
+                                    if constexpr (NA > 1) a1 = g.n_acc > 1 ? acc[i + u][1] : 0ll;
+                                    v[u] = acc2_to_double_rn(acc[i + u][0], a1, B1, es[i + u], bJ1);
+                                } else {
+                                    uint32_t q[W];
+                                    exact_q(i + u, q);
+                                    v[u] = q_to_double<W>(q, es[i + u], bJ1, g.out_mode);
+                                }
                                 // BLAS semantics: C is not read when beta == 0
                                 if (!plain)
                                     v[u] = g.beta == 0.0 ? g.alpha * v[u] : fma(g.beta, crow[col], g.alpha * v[u]);
