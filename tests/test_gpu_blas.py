@@ -113,3 +113,21 @@ def test_host_arrays_split_launch_bit_identical(gpu_handle, oracle, ozlib):
     for r0 in (0, 1023, 2047, 2048, 2999):
         ref = oracle.dgemm_rows(A, B, 7, 9, 9, 0, r0, r0 + 1)
         assert np.array_equal(C[r0:r0 + 1].view(np.uint64), ref.view(np.uint64)), r0
+
+
+@pytest.mark.parametrize("ta,tb", [(1, 0), (0, 1), (1, 1)])
+def test_transposes_e4m3_slices_bit_identical(gpu_handle, oracle, ta, tb):
+    """Transposed operands with 4-bit slices (e4m3 carrier): the transposed split
+    jobs keep the oracle's bits."""
+    M, N, K = 150, 97, 333
+    opA = oracle.gen_phi((M, K), 97, 1.0)
+    opB = oracle.gen_phi((K, N), 98, 1.0)
+    A_st, lda = _store(opA, ta, 5)
+    B_st, ldb = _store(opB, tb, 3)
+    gpu_handle.set_bits(4)
+    gpu_handle.set_slices(12)
+    gpu_handle.set_bins(12)
+    C = _ex(gpu_handle, ta, tb, M, N, K, 1.0, A_st, lda, B_st, ldb, 0.0, np.full((M, N), np.nan), N)
+    assert gpu_handle.config()["slice_format"] == 1
+    ref = oracle.dgemm(opA, opB, 4, 12, 12, 0)
+    assert np.array_equal(C.view(np.uint64), ref.view(np.uint64))
