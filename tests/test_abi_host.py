@@ -219,3 +219,18 @@ def test_tuning_table_starts_empty_and_clears(ozlib):
     # a host-only plan query never consults or fills the table
     assert ozlib.plan_query(1024, 1024, 1024, 7, 9, 9) is not None
     assert api.tuning_entries() == 0
+
+
+@pytest.mark.parametrize("b,s,J", [(4, 10, 10), (3, 18, 18), (4, 8, 15), (3, 29, 29), (2, 12, 12), (7, 9, 9)])
+def test_plan_slice_format(ozlib, b, s, J):
+    """Slices of b <= 4 bits plan on e4m3 (chunks of 32 or 64 K values), wider ones
+    on bf16 (16 or 32); the fp32 exactness bound holds with the carrier's chunk."""
+    M, N, K = 4096, 4096, 4096
+    c = ozlib.plan_query(M, N, K, b, s, J)
+    assert c is not None
+    if b <= 4:
+        assert c["slice_format"] == 1 and c["k_chunk"] in (32, 64)
+    else:
+        assert c["slice_format"] == 0 and c["k_chunk"] in (16, 32)
+    max_pairs = max(_pairs(s, j + 1) - _pairs(s, j) for j in range(J))
+    assert max_pairs * c["k_chunk"] * c["drain_chunks"] * (2 ** b - 1) ** 2 <= 2 ** 24
