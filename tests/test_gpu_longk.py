@@ -101,3 +101,43 @@ def test_partial_wave_split_bit_exact(ozlib, oracle):
         for r0, ref in refs.items():
             assert np.array_equal(C[r0:r0 + 1].view(np.uint64), ref.view(np.uint64)), r0
     h.close()
+
+
+def test_split_wave_alpha_beta_and_reference_decode(ozlib, oracle):
+    """The K-split's completing part runs the same epilogue as a whole tile: with
+    C = alpha AB + beta C (beta read once) and with the reference's truncating
+    decode (reference profile, e4m3 slices of 3 bits)."""
+    import torch
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream().cuda_stream
+    # 12 tiles of 128 x 48 with 64 chunks: each tile split along K
+    M, N, K = 256, 288, 2048
+    A = oracle.gen_phi((M, K), 51, 1.0)
+    B = oracle.gen_phi((K, N), 52, 1.0)
+    C0 = oracle.gen_uniform((M, N), 53)
+    dA, dB, dC = (torch.from_numpy(x).to(dev) for x in (A, B, C0))
+    h = ozlib.Handle()
+    h.set_slices(9)
+    h.set_bins(9)
+    alpha, beta = -1.5, 0.25
+    assert h.dgemm_ex(0, 0, M, N, K, alpha, dA.data_ptr(), K, dB.data_ptr(), N, beta, dC.data_ptr(), N, stream) == 0
+    assert h.sync() == 0, h.last_error()
+    h.close()
+    x = oracle.dgemm(A, B, 7, 9, 9, 0)
+    want = alpha * x + beta * C0
+    scale = np.maximum(np.abs(alpha * x), np.abs(beta * C0))
+    assert np.all(np.abs(dC.cpu().numpy() - want) <= 2 * np.spacing(scale))
+    # reference profile: K = 4096 picks (b, d) = (3, 25) from the reference's table
+    M, N, K = 128, 384, 4096
+    A = oracle.gen_phi((M, K), 54, 1.0)
+    B = oracle.gen_phi((K, N), 55, 1.0)
+    h = ozlib.Handle()
+    h.set_profile(1)
+    assert h.setup(M, N, K, 0) == 0, h.last_error()
+    C = np.empty((M, N))
+    assert h.dgemm(M, N, K, A, B, C) == 0, h.last_error()
+    cfg = h.config()
+    h.close()
+    assert cfg["slice_format"] == 1 and cfg["bits"] == 3
+    ref = oracle.dgemm(A, B, cfg["bits"], cfg["slices"], cfg["bins"], 1)
+    assert np.array_equal(C.view(np.uint64), ref.view(np.uint64))
