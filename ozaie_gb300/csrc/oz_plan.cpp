@@ -109,7 +109,7 @@ std::map<PlanKey, Plan> g_plans;
 
 bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string *err, int bin_lo, int bin_hi,
                const PlanHints *hints) {
-    if (hints || std::getenv("OZGB_KC") || std::getenv("OZGB_GROUPS"))
+    if (hints)
         return make_plan_uncached(M, N, K, cfg, out, err, bin_lo, bin_hi, hints);
     long gen;
     {
@@ -246,8 +246,7 @@ bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std
     // block spans the whole block (zero B slices pad the out-of-range q).  Measured
     // on GB300: one M=128 K=16 UMMA costs max(~114, N/2) cycles, so the partition
     // minimising sum(#A slices x cost(N)) is chosen by dynamic programming.
-    const char *env_g = std::getenv("OZGB_GROUPS");
-    const int max_groups = std::min(kMaxGroups, env_g ? std::max(1, std::atoi(env_g)) : kMaxGroups);
+    const int max_groups = kMaxGroups;
     const int maxb = 256 / p.BN;
     auto p0_of = [s](int lo) { return std::max(0, lo - (s - 1)); };
     auto p1_of = [s](int hi) { return std::min(hi, s - 1); };
@@ -291,7 +290,7 @@ bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std
             i = k;
         }
     }
-    if (!hint.groups && !std::getenv("OZGB_GROUPS")) {
+    if (!hint.groups) {
         // Drain-aware choice among the cost model's best partition per block count
         // and every two-block split.  A block drained after a chunk must be read out
         // (about 0.1 SM cycles per value: 16 F2I conversions per cycle) before its
@@ -398,8 +397,7 @@ bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std
     const size_t budget = kSmemLimit - kSmemReserve;
     const int kc_opts[2] = {p.f8 ? 64 : 32, p.f8 ? 32 : 16};
     const int kmin = kc_opts[1];
-    const char *env_kc = std::getenv("OZGB_KC");  // tuning override
-    const int force_kc = hint.KC ? hint.KC : (env_kc ? std::atoi(env_kc) : 0);
+    const int force_kc = hint.KC;
     auto stage_of = [&](int kc) {
         return (static_cast<size_t>(s) * BM * kc + static_cast<size_t>(p.pad_lo + s + p.pad_hi) * p.BN * kc) * eb;
     };
