@@ -89,12 +89,15 @@ def test_bad_leading_dimension(gpu_handle):
     assert gpu_handle.dgemm_ex(1, 0, 8, 4, 4, 1.0, p, 4, p, 4, 0.0, p, 4) == 7  # lda < M for op(A) = A^T
 
 
-def test_host_arrays_split_launch_bit_identical(gpu_handle, oracle, ozlib):
+@pytest.mark.parametrize("M,N,K,rows", [
+    (3000, 2048, 256, (0, 1023, 2047, 2048, 2999)),   # 24 row tiles: split after two groups
+    (2048, 1104, 256, (0, 1023, 1024, 2047)),         # second launch: 64 tiles, each split along K
+])
+def test_host_arrays_split_launch_bit_identical(gpu_handle, oracle, ozlib, M, N, K, rows):
     """Host-array calls with more than one group of 8 row tiles run the GEMM as two
     launches and copy the first rows of C back during the second: the result is
     the bits of the device-pointer call (and of the oracle on sampled rows)."""
     import torch
-    M, N, K = 3000, 2048, 256  # 24 row tiles: three groups, split after two
     A = oracle.gen_phi((M, K), 91, 1.0)
     B = oracle.gen_phi((K, N), 92, 1.0)
     gpu_handle.set_slices(9)
@@ -110,7 +113,7 @@ def test_host_arrays_split_launch_bit_identical(gpu_handle, oracle, ozlib):
     want = _ex(h, 0, 0, M, N, K, 1.0, A, K, B, N, 0.0, np.full((M, N), np.nan), N)
     h.close()
     assert np.array_equal(C.view(np.uint64), want.view(np.uint64))
-    for r0 in (0, 1023, 2047, 2048, 2999):
+    for r0 in rows:
         ref = oracle.dgemm_rows(A, B, 7, 9, 9, 0, r0, r0 + 1)
         assert np.array_equal(C[r0:r0 + 1].view(np.uint64), ref.view(np.uint64)), r0
 
