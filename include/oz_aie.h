@@ -17,7 +17,7 @@
 //     reference silently overruns its buffers), 5 when setup was never called;
 //   * every function is inline: the header can be included by several
 //     translation units (the reference defines non-inline globals).
-// Link with liboz_gb300.so (see INTEGRATION.md for the CMake helper).
+// Link with liboz_gb300.so (include/CMakeLists.txt provides use_ozaie(target)).
 #pragma once
 
 #include <cstdint>

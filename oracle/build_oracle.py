@@ -4,7 +4,9 @@ Builds
   oracle/liboz_oracle.so        -- the CPU restatement (oz_oracle.c), gcc + OpenMP
   oracle/_ref/libref_decode.so  -- the reference's own convert_paired_i64_to_double_matrix
                                    (include/oz_aie.h:92-150), only when the reference
-                                   sources are present at REFERENCE_ROOT.
+                                   sources are present at REFERENCE_ROOT: the
+                                   environment variable OZAIE_REFERENCE_ROOT, else a
+                                   checkout named "reference" beside this repository.
 
 Outputs go only to oracle/ and oracle/_ref/ (both git-ignored binaries).
 """
@@ -14,7 +16,8 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE_ROOT = os.environ.get("OZAIE_REFERENCE_ROOT", "/root/reference")
+REFERENCE_ROOT = os.environ.get("OZAIE_REFERENCE_ROOT") or os.path.join(
+    os.path.dirname(os.path.dirname(HERE)), "reference")
 ORACLE_SO = os.path.join(HERE, "liboz_oracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_SO = os.path.join(REF_DIR, "libref_decode.so")

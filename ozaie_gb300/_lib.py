@@ -104,7 +104,7 @@ SIGNATURES = [
 
 def lib_path():
     """liboz_gb300.so in the package directory, or the path in OZGB_LIB_PATH
-    (an alternative build of the same library, e.g. one with cycle probes)."""
+    (an alternative build of the same library)."""
     return os.environ.get("OZGB_LIB_PATH") or _build.LIB
 
 

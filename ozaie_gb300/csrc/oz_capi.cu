@@ -479,19 +479,6 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
         g.acc_t0[0] = 0;
         g.acc_t0[1] = g.pair_g0;
     }
-#ifdef OZGB_PROBE
-    // probe builds: per-CTA cycle counters of the GEMM roles, summarised on stderr
-    static unsigned long long *probe = nullptr;
-    static size_t probe_n = 0;
-    const size_t need = static_cast<size_t>(p.tiles_m) * p.tiles_n * 8;
-    if (probe_n < need) {
-        if (probe) cudaFree(probe);
-        cudaMalloc(&probe, need * 8);
-        probe_n = need;
-    }
-    cudaMemsetAsync(probe, 0, need * 8, st);
-    g.probe = probe;
-#endif
     const int total = p.tiles_m * p.tiles_n;
     int t_split = 0, rows_split = 0;
     if (ho && (out_mode == OUT_RN || out_mode == OUT_RZ_REF) && o.ldc == o.N) {
@@ -541,22 +528,6 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
     h->launches += 1;
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(h, e, "slice-pair GEMM launch");
-#ifdef OZGB_PROBE
-    {
-        cudaStreamSynchronize(st);
-        std::vector<unsigned long long> hp(need);
-        cudaMemcpy(hp.data(), probe, need * 8, cudaMemcpyDeviceToHost);
-        double sum[8] = {0};
-        for (size_t i = 0; i < need; ++i) sum[i % 8] += static_cast<double>(hp[i]);
-        const double n = static_cast<double>(need / 8);
-        fprintf(stderr,
-                "OZGB_PROBE tiles=%.0f cycles per tile (CTA sums / tiles): producer_wait=%.0f mma_wait_full=%.0f "
-                "mma_wait_drained=%.0f mma_issue=%.0f drain_wait=%.0f drain_work=%.0f epilogue=%.0f total=%.0f "
-                "(n_kc=%d blocks=%d)\n",
-                n, sum[0] / n, sum[1] / n, sum[2] / n, sum[3] / n, sum[4] / n, sum[5] / n, sum[6] / n, sum[7] / n,
-                p.n_kc, p.G);
-    }
-#endif
     return OZGB_OK;
 }
 

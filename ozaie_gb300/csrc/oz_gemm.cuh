@@ -51,6 +51,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "oz_internal.h"
 #include "oz_ptx.cuh"
 
@@ -284,15 +286,6 @@ struct DrainSchedule {
     }
 };
 
-// Optional cycle probes (OZGB_PROBE builds only).
-#ifdef OZGB_PROBE
-#define OZ_PT(name) long long name = clock64()
-#define OZ_PADD(acc, t0) (acc) += clock64() - (t0)
-#else
-#define OZ_PT(name)
-#define OZ_PADD(acc, t0)
-#endif
-
 // ------------------------------------------------------------------ kernel
 // The operands and output of one tile and its position.  Grouped rasterisation:
 // 8 M-tiles share the same stream of B tiles.
@@ -378,10 +371,6 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
     int *split_flag = blk_np + kMaxGroups;  // this CTA's part completed a split tile
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-#ifdef OZGB_PROBE
-    long long pr0 = 0, pr1 = 0, pr2 = 0, pr3 = 0;
-    const long long pstart = clock64();
-#endif
 
     // zero B slices below and above the loaded ones (read by out-of-range pairs)
     {
@@ -431,9 +420,7 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
             // the (r-1)-th release of that stage
             auto acquire = [&]() -> bool {
                 const long long r = issued / g.stages;
-                OZ_PT(tw);
                 const bool got = (r == 0) || mbar_wait(&empty[st], static_cast<uint32_t>((r - 1) & 1), vabort, TO);
-                OZ_PADD(pr0, tw);
                 if (!got && !*vabort) {
                     atomicCAS(g.err, 0, DEVERR_TIMEOUT_PRODUCER);
                     *vabort = 1;
@@ -513,15 +500,12 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
             uint32_t fparity = 0;
             bool ok = true;
             for (;;) {
-                OZ_PT(tf);
                 const bool gotf = mbar_wait(&full[st], fparity, vabort, TO);
-                OZ_PADD(pr0, tf);
                 if (!gotf) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
-                OZ_PT(ti);
                 const uint64_t stage_off = (static_cast<uint64_t>(st) * g.stage_bytes) >> 4;
                 const uint32_t cur = stage_mask[st];
                 if (cur & kStageTerminate) break;
@@ -535,10 +519,8 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                         const uint32_t bit = 1u << blk;
                         m &= m - 1;
                         if (cls == 2) {
-                            OZ_PT(te);
                             const bool gote = mbar_wait(&gempty[blk],
                                                         static_cast<uint32_t>((ephase >> blk) & 1ull), vabort, TO);
-                            OZ_PADD(pr1, te);
                             if (!gote) {
                                 ok = false;
                                 break;
@@ -574,7 +556,6 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                         }
                     }
                 }
-                OZ_PADD(pr2, ti);
                 if (!ok) break;
                 umma_commit(&empty[st]);
                 if (++st == g.stages) {
@@ -632,17 +613,14 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                     while (m) {
                         const int blk = __ffs(m) - 1;
                         m &= m - 1;
-                        OZ_PT(tg);
                         const bool gotg =
                             mbar_wait(&gfull[blk], static_cast<uint32_t>((fphase >> blk) & 1ull), vabort, TO);
-                        OZ_PADD(pr0, tg);
                         if (!gotg) {
                             ok = false;
                             break;
                         }
                         fphase ^= (1ull << blk);
                         tc_fence_after();
-                        OZ_PT(td);
                         int lo = 0, nb = 0;  // static-index selects (see the MMA issuer)
 #pragma unroll
                         for (int i = 0; i < kMaxGroups; ++i)
@@ -676,7 +654,6 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                         tc_fence_before();
                         __syncwarp();
                         if (lane == 0) mbar_arrive(&gempty[blk]);
-                        OZ_PADD(pr1, td);
                     }
                 }
                 prev = cur;
@@ -725,7 +702,6 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
             }
 
             // --------------------------------------------------- epilogue
-            OZ_PT(tq);
             const int row = tr.mt * BM + 32 * qd + lane;
             const int col0 = tr.nt * BN + part * COLS;
             if (row < tr.M) {
@@ -817,7 +793,6 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                     }
                 }
             }
-            OZ_PADD(pr2, tq);
         }
         if (!ok && !*vabort) {
             atomicCAS(g.err, 0, DEVERR_TIMEOUT_EPI);
@@ -826,15 +801,6 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
     }
 
     __syncthreads();
-#ifdef OZGB_PROBE
-    if (g.probe && lane == 0 && warp <= 2) {
-        unsigned long long *pp = g.probe + static_cast<size_t>(blockIdx.x) * 8;
-        if (warp == 0) { pp[0] = pr0; pp[7] = clock64() - pstart; }
-        if (warp == 1) { pp[1] = pr0; pp[2] = pr1; pp[3] = pr2; }
-        if (warp == 2) { pp[4] = pr0; pp[5] = pr1; pp[6] = pr2; }
-    }
-    (void)pr3;
-#endif
     if (warp == 1) {
         tc_fence_after();
         tmem_dealloc(tmem, g.tmem_cols);
@@ -861,16 +827,17 @@ void launch_gemm_variant(const GemmArgs &args, int tiles, size_t smem, void *str
     auto kern = oz_gemm_kernel<BN, W, KC, F8>;
     // the shared-memory limit is raised once per device to the opt-in maximum (a
     // per-launch attribute call costs more than the launch itself; every caller
-    // sets the same value, so concurrent first calls do not conflict)
-    static bool raised[64] = {false};
+    // sets the same value, so two host threads that both make the first call only
+    // repeat the same attribute call)
+    static std::atomic<bool> raised[64] = {};
     int dev = 0;
     cudaGetDevice(&dev);
-    if (dev < 0 || dev >= 64 || !raised[dev]) {
+    if (dev < 0 || dev >= 64 || !raised[dev].load(std::memory_order_acquire)) {
         int opt = 0;
         cudaDeviceGetAttribute(&opt, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              opt > static_cast<int>(smem) ? opt : static_cast<int>(smem));
-        if (dev >= 0 && dev < 64) raised[dev] = true;
+        if (dev >= 0 && dev < 64) raised[dev].store(true, std::memory_order_release);
     }
     const int range = args.total_tiles - args.tile_begin;
     const int grid = range < device_sm_count() ? range : device_sm_count();

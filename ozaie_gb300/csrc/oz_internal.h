@@ -69,10 +69,6 @@ struct GemmArgs {
     uint32_t tmem_cols;
     int *err;
     unsigned long long timeout_ns;
-    // Per-CTA cycle counters, written only by builds with OZGB_PROBE defined
-    // (8 slots per CTA: producer wait, MMA wait full / wait drained / issue,
-    // drain wait / work, epilogue, total); null otherwise.
-    unsigned long long *probe;
     // Bin blocks (also the drain groups).  Block g holds bins [lo, lo + nb);
     // every UMMA of the block covers all of its bins (one accumulator range):
     // A slice p in [p0, p1] against B slices q = j - p, the out-of-range q

@@ -19,6 +19,12 @@
 // each call clears what must start at zero (the column exponents and the error
 // word).  Calls whose executions overlap on the GPU (other streams, other host
 // threads) race on the array and corrupt each other's results.
+//
+// The status covers argument checks and launches only: the call returns before
+// the kernels run.  A device-side wait that runs out of time (the GEMM stops
+// early and leaves C incomplete) is recorded in the array's error word, which
+// this entry point does not read back and the next call clears.  A caller that
+// must detect that case uses ozgb_dgemm_device and ozgb_sync instead.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -95,6 +101,9 @@ extern "C" ozgb_status ozgb_dgemm_device_noalloc(int M, int N, int K, const doub
     const size_t need = off_bt + round256(p.b_bytes);
     if (need > kNoAllocScratchBytes) return OZGB_ERR_TOO_LARGE;
 
+    // an error left pending by earlier, unrelated work on this thread is cleared
+    // here, so that the checks below report only what this call launched
+    cudaGetLastError();
     unsigned char *base = nullptr;
     const ozgb_status rc = scratch_base(&base);
     if (rc != OZGB_OK) return rc;
@@ -115,6 +124,7 @@ extern "C" ozgb_status ozgb_dgemm_device_noalloc(int M, int N, int K, const doub
     launch_colmax(dB, ldb, K, N, ec, nullptr, st);
     launch_split_a(dA, lda, M, K, er, p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.Mp, at, st, false, p.f8);
     launch_split_b(dB, ldb, K, N, ec, p.cfg.b, p.cfg.s, p.KC, p.n_kc, p.BN, p.Np, bt, st, false, p.f8);
+    if (cudaGetLastError() != cudaSuccess) return OZGB_ERR_EXEC;  // a stage (a) or (b) launch
 
     GemmArgs g;
     std::memset(&g, 0, sizeof g);
@@ -159,6 +169,6 @@ extern "C" ozgb_status ozgb_dgemm_device_noalloc(int M, int N, int K, const doub
         g.blk_off[i] = p.blk_off[i];
     }
     p.fn(g, p.tiles_m * p.tiles_n, p.smem, st);
-    if (cudaGetLastError() != cudaSuccess) return OZGB_ERR_EXEC;
+    if (cudaGetLastError() != cudaSuccess) return OZGB_ERR_EXEC;  // the slice-pair GEMM launch
     return OZGB_OK;
 }
