@@ -168,9 +168,23 @@ ozgb_status ozgb_set_rounding(ozgb_handle h, int rounding);
 /* Slice format: 0 = e4m3 where it is exact (b <= 4) and a kernel fits, else bf16
  * (default); 1 = bf16 always. */
 ozgb_status ozgb_set_slice_format(ozgb_handle h, int format);
-/* Requested normwise relative error (> 0 enables slice selection from the
- * exponent spread measured by stage (a)); 0 disables it. */
+/* Requested relative error (> 0 enables slice selection from the exponent
+ * spread measured by stage (a)); 0 disables it.  The error it bounds is set by
+ * ozgb_set_error_criterion (normwise by default). */
 ozgb_status ozgb_set_error_bound(ozgb_handle h, double bound);
+/* Which error the precision knob bounds.  No reference counterpart (the
+ * reference fixes s per shape, include/oz_aie.h:60-80; its harness reports the
+ * largest elementwise relative error against MPFR, common.h:585-592).
+ *   OZGB_CRIT_NORMWISE (default): |C^ - C|_F / |C|_F.
+ *   OZGB_CRIT_ELEMENTWISE: |c^_ij - c_ij| / |c_ij| for every entry with
+ *     |c_ij| >= tail * |a_i| |b_j| / sqrt(K) (row i of op(A), column j of
+ *     op(B)).  An entry that cancels to near zero has no relative error bound at
+ *     any fixed precision; `tail` (in (0, 1], e.g. 1e-4) leaves out the entries
+ *     within that distance of zero, about a tail's fraction of them for random
+ *     signs and moderate spreads. 
+ * Both are a-priori estimates from the stage-(a) statistics, not guarantees. */
+enum { OZGB_CRIT_NORMWISE = 0, OZGB_CRIT_ELEMENTWISE = 1 };
+ozgb_status ozgb_set_error_criterion(ozgb_handle h, int criterion, double tail);
 ozgb_status ozgb_set_graph(ozgb_handle h, int enable);     /* capture grouped calls in CUDA graphs */
 ozgb_status ozgb_set_timeout_ms(ozgb_handle h, double ms); /* device-side wait limit, default 2000 */
 ozgb_status ozgb_get_config(ozgb_handle h, ozgb_config *out);
@@ -239,6 +253,10 @@ int ozgb_plan_query(int M, int N, int K, int bits, int slices, int bins, ozgb_co
  * input. */
 int ozgb_choose_slices(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N,
                        const double *sa_k, const double *sb_k, int K, int bits, double bound, double *estimate);
+/* The same with a criterion and tail as in ozgb_set_error_criterion. */
+int ozgb_choose_slices_ex(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N,
+                          const double *sa_k, const double *sb_k, int K, int bits, double bound, int criterion,
+                          double tail, double *estimate);
 
 /* Library version string. */
 const char *ozgb_version(void);

@@ -79,6 +79,7 @@ SIGNATURES = [
     ("ozgb_set_rounding", _i, [_h, _i]),
     ("ozgb_set_slice_format", _i, [_h, _i]),
     ("ozgb_set_error_bound", _i, [_h, _dbl]),
+    ("ozgb_set_error_criterion", _i, [_h, _i, _dbl]),
     ("ozgb_set_graph", _i, [_h, _i]),
     ("ozgb_set_timeout_ms", _i, [_h, _dbl]),
     ("ozgb_get_config", _i, [_h, ctypes.POINTER(OzgbConfig)]),
@@ -90,6 +91,7 @@ SIGNATURES = [
     ("ozgb_convert_paired_i64_to_double", _i, [_p, _p, _i, _i, _i, _i, _i]),
     ("ozgb_plan_query", _i, [_i, _i, _i, _i, _i, _i, ctypes.POINTER(OzgbConfig)]),
     ("ozgb_choose_slices", _i, [_p, _p, _i, _p, _p, _i, _p, _p, _i, _i, _dbl, ctypes.POINTER(_dbl)]),
+    ("ozgb_choose_slices_ex", _i, [_p, _p, _i, _p, _p, _i, _p, _p, _i, _i, _dbl, _i, _dbl, ctypes.POINTER(_dbl)]),
     ("ozgb_dgemm_device_noalloc", _i, [_i, _i, _i, _p, ctypes.c_long, _p, ctypes.c_long, _p, ctypes.c_long, _i, _p]),
     ("ozgb_dgemm_ex", _i, [_h, _i, _i, _i, _i, _i, _dbl, _p, ctypes.c_long, _p, ctypes.c_long, _dbl, _p,
                            ctypes.c_long, _p]),

@@ -29,6 +29,11 @@ class Profile(enum.IntEnum):
     reference = 1
 
 
+class Criterion(enum.IntEnum):
+    normwise = 0
+    elementwise = 1
+
+
 class Rounding(enum.IntEnum):
     default = -1
     nearest = 0
@@ -141,6 +146,10 @@ class Handle:
     def set_error_bound(self, e):
         return self._check(self._L.ozgb_set_error_bound(self._h, float(e)))
 
+    def set_error_criterion(self, criterion, tail=1e-4):
+        """Criterion.normwise (default) or Criterion.elementwise with its tail."""
+        return self._check(self._L.ozgb_set_error_criterion(self._h, int(criterion), float(tail)))
+
     def set_graph(self, on):
         return self._check(self._L.ozgb_set_graph(self._h, 1 if on else 0))
 
@@ -239,10 +248,12 @@ def plan_query(M, N, K, bits, slices, bins):
     return None if rc else c.as_dict()
 
 
-def choose_slices(er, ssr, ec, ssc, K, bits, bound, sa_k=None, sb_k=None):
+def choose_slices(er, ssr, ec, ssc, K, bits, bound, sa_k=None, sb_k=None, criterion=0, tail=1e-4):
     """Host-only precision knob: (slice count, a-priori error estimate) for a
-    requested normwise bound, from the stage-(a) statistics.  sa_k / sb_k are the
-    sums of squares of the columns of A and the rows of B (None: spread evenly)."""
+    requested bound, from the stage-(a) statistics.  sa_k / sb_k are the sums of
+    squares of the columns of A and the rows of B (None: spread evenly);
+    criterion 0 bounds the normwise error, 1 the elementwise error of the
+    entries at least tail sigma_ij away from zero."""
     er = np.ascontiguousarray(er, np.int32)
     ec = np.ascontiguousarray(ec, np.int32)
     ssr = np.ascontiguousarray(ssr, np.float64)
@@ -250,9 +261,9 @@ def choose_slices(er, ssr, ec, ssc, K, bits, bound, sa_k=None, sb_k=None):
     ka = None if sa_k is None else np.ascontiguousarray(sa_k, np.float64)
     kb = None if sb_k is None else np.ascontiguousarray(sb_k, np.float64)
     est = ctypes.c_double()
-    s = load().ozgb_choose_slices(_ptr(er), _ptr(ssr), er.size, _ptr(ec), _ptr(ssc), ec.size,
-                                  None if ka is None else _ptr(ka), None if kb is None else _ptr(kb), int(K),
-                                  int(bits), float(bound), ctypes.byref(est))
+    s = load().ozgb_choose_slices_ex(_ptr(er), _ptr(ssr), er.size, _ptr(ec), _ptr(ssc), ec.size,
+                                     None if ka is None else _ptr(ka), None if kb is None else _ptr(kb), int(K),
+                                     int(bits), float(bound), int(criterion), float(tail), ctypes.byref(est))
     return s, est.value
 
 

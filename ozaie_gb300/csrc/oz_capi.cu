@@ -60,6 +60,8 @@ struct ozgb_context {
     int profile = OZGB_PROFILE_GB300;
     int opt_bits = 0, opt_slices = 0, opt_bins = 0, opt_rounding = OZGB_ROUND_DEFAULT, opt_format = 0;
     double err_bound = 0.0;
+    int err_crit = KNOB_NORMWISE;  // precision knob: normwise or elementwise criterion
+    double err_tail = 1e-4;        // elementwise: entries within err_tail sigma of zero left out
     int use_graph = 0;
     unsigned long long timeout_ns = 2000000000ull;
     // last effective plan
@@ -287,7 +289,7 @@ ozgb_status choose_config(ozgb_handle h, const Operands &o, int mode, cudaStream
     if (h->err_bound > 0.0 && h->opt_slices <= 0) {
         // precision knob: the stage-(a) partial sums are reduced on the device to
         // five scaled sums, and only those cross to the host
-        if (!h->knob.ensure(5 * sizeof(double))) return fail(h, OZGB_ERR_ALLOC, "knob buffer");
+        if (!h->knob.ensure(sizeof(KnobStats))) return fail(h, OZGB_ERR_ALLOC, "knob buffer");
         KnobJob j = h->kjob;
         j.out = static_cast<double *>(h->knob.p);
         launch_knob_stats(j, st);
@@ -297,7 +299,7 @@ ozgb_status choose_config(ozgb_handle h, const Operands &o, int mode, cudaStream
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return cuda_fail(h, e, "statistics readback");
         double est = 0;
-        const int s = choose_slices_stats(ks, o.K, cfg->b, h->err_bound, 2, 16, &est);
+        const int s = choose_slices_stats(ks, o.K, cfg->b, h->err_bound, 2, 16, &est, h->err_crit, h->err_tail);
         cfg->s = s;
         cfg->J = s;
     }
@@ -781,7 +783,8 @@ ozgb_status enqueue_grouped(ozgb_handle h, ozgb_problem *probs, int n, int mode,
         if (e != cudaSuccess) return cuda_fail(h, e, "grouped statistics readback");
         for (int i = 0; i < n; ++i)
             if (bound[i] > 0.0)
-                s_pick[i] = choose_slices_stats(h->knob_host[adapt_idx[i]], probs[i].K, 7, bound[i], 2, 16, nullptr);
+                s_pick[i] = choose_slices_stats(h->knob_host[adapt_idx[i]], probs[i].K, 7, bound[i], 2, 16, nullptr,
+                                                h->err_crit, h->err_tail);
     }
 
     // ---- plans
@@ -1131,6 +1134,15 @@ ozgb_status ozgb_set_error_bound(ozgb_handle h, double bound) {
     h->err_bound = bound;
     return OZGB_OK;
 }
+ozgb_status ozgb_set_error_criterion(ozgb_handle h, int criterion, double tail) {
+    if (!h || (criterion != OZGB_CRIT_NORMWISE && criterion != OZGB_CRIT_ELEMENTWISE) || !(tail > 0.0) ||
+        !(tail <= 1.0))
+        return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->err_crit = criterion;
+    h->err_tail = tail;
+    return OZGB_OK;
+}
 ozgb_status ozgb_set_graph(ozgb_handle h, int enable) {
     if (!h) return OZGB_ERR_ARG;
     std::lock_guard<std::mutex> lk(h->mu);
@@ -1441,9 +1453,18 @@ int ozgb_plan_query(int M, int N, int K, int bits, int slices, int bins, ozgb_co
 
 int ozgb_choose_slices(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N,
                        const double *sa_k, const double *sb_k, int K, int bits, double bound, double *estimate) {
+    return ozgb_choose_slices_ex(er, ssr, M, ec, ssc, N, sa_k, sb_k, K, bits, bound, OZGB_CRIT_NORMWISE, 1e-4,
+                                 estimate);
+}
+
+int ozgb_choose_slices_ex(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N,
+                          const double *sa_k, const double *sb_k, int K, int bits, double bound, int criterion,
+                          double tail, double *estimate) {
     if (!er || !ssr || !ec || !ssc || M < 1 || N < 1 || K < 1 || bits < 1 || !(bound > 0)) return -1;
+    if ((criterion != OZGB_CRIT_NORMWISE && criterion != OZGB_CRIT_ELEMENTWISE) || !(tail > 0.0) || !(tail <= 1.0))
+        return -1;
     const KnobStats ks = knob_stats_host(er, ssr, M, ec, ssc, N, sa_k, sb_k, K);
-    return choose_slices_stats(ks, K, bits, bound, 2, 16, estimate);
+    return choose_slices_stats(ks, K, bits, bound, 2, 16, estimate, criterion, tail);
 }
 
 }  // extern "C"

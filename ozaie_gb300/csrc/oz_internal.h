@@ -145,7 +145,7 @@ struct KnobJob {
     int N;
     int K;
     StatParts ra, cb, ka, kb;
-    double *out;  // 5 doubles, zeroed before
+    double *out;  // the 7 doubles of KnobStats (oz_plan.h), zeroed before
 };
 
 // Device error codes written to the error word.
@@ -178,7 +178,7 @@ void launch_split_a(const double *A, long lda, int M, int K, const int32_t *er, 
 void launch_split_b(const double *B, long ldb, int K, int N, const int32_t *ec, int b, int s, int KC, int n_kc,
                     int BN, int Np, uint16_t *tiles, void *stream, bool trans = false, bool f8 = false);
 int launch_selftest_timeout(int *err, unsigned long long timeout_ns, void *stream);
-// Precision-knob statistics (five doubles, see KnobStats in oz_plan.h) of one
+// Precision-knob statistics (seven doubles, KnobStats in oz_plan.h) of one
 // problem; zeroes j.out first.
 void launch_knob_stats(const KnobJob &j, void *stream);
 // Grid sizes of the per-problem stage kernels (blocks in x and y of 256 threads).

@@ -561,8 +561,15 @@ std::vector<PlanHints> plan_candidates(int M, int N, int K, const OzConfig &cfg,
     return kept;
 }
 
-double knob_estimate(const KnobStats &k, int K, int b, int s) {
+double knob_estimate(const KnobStats &k, int K, int b, int s, int crit, double tail) {
     const double safety = 1.5;
+    if (crit == KNOB_ELEMENTWISE) {
+        if (!(k.ia > 0.0) || !(k.ib > 0.0) || !(tail > 0.0)) return HUGE_VAL;
+        const double Kd = static_cast<double>(K);
+        const double r = Kd * (s - 1.0) * (s - 1.0) * k.ia * k.ib / 16.0 + (k.ia + k.ib) / 3.0;
+        const double v = safety * std::ldexp(std::sqrt(Kd * r), -b * s) / tail + std::ldexp(1.0, -53);
+        return std::isfinite(v) ? v : HUGE_VAL;
+    }
     if (!(k.t > 0.0)) return HUGE_VAL;
     const double dropped = 0.25 * (s - 1.0) * std::sqrt(static_cast<double>(K) * k.sa * k.sb);
     const double tails = std::sqrt(k.sa * k.nb / 3.0) + std::sqrt(k.sb * k.na / 3.0);
@@ -570,11 +577,12 @@ double knob_estimate(const KnobStats &k, int K, int b, int s) {
     return std::isfinite(v) ? v : HUGE_VAL;
 }
 
-int choose_slices_stats(const KnobStats &k, int K, int b, double bound, int s_min, int s_max, double *estimate) {
+int choose_slices_stats(const KnobStats &k, int K, int b, double bound, int s_min, int s_max, double *estimate,
+                        int crit, double tail) {
     int s = s_min;
     double est = HUGE_VAL;
     for (; s <= s_max; ++s) {
-        est = knob_estimate(k, K, b, s);
+        est = knob_estimate(k, K, b, s, crit, tail);
         if (est <= bound) break;
     }
     if (s > s_max) s = s_max;
@@ -603,8 +611,15 @@ KnobStats knob_stats_host(const int32_t *er, const double *ssr, int M, const int
     } else {
         t = na * nb / K;
     }
+    // the flattest row and column: max 1 / (|x|^2 4^{1022-E}) over the non-zero units
+    long double ia = 0, ib = 0;
+    for (int i = 0; i < M; ++i)
+        if (ssr[i] > 0) ia = std::max(ia, 1.0L / std::ldexp(static_cast<long double>(ssr[i]), 2 * (1022 - er[i])));
+    for (int j = 0; j < N; ++j)
+        if (ssc[j] > 0) ib = std::max(ib, 1.0L / std::ldexp(static_cast<long double>(ssc[j]), 2 * (1022 - ec[j])));
     return KnobStats{static_cast<double>(sa), static_cast<double>(na), static_cast<double>(sb),
-                     static_cast<double>(nb), static_cast<double>(t)};
+                     static_cast<double>(nb), static_cast<double>(t),  static_cast<double>(ia),
+                     static_cast<double>(ib)};
 }
 
 }  // namespace ozgb

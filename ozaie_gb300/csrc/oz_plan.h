@@ -85,10 +85,19 @@ void reference_table(int K, int mode, int *b, int *d);
 // largest column exponent eb of B:
 //   sa = sum_i 4^{Er_i-ea},  na = ||A||_F^2 4^{1022-ea},
 //   sb = sum_j 4^{Ec_j-eb},  nb = ||B||_F^2 4^{1022-eb},
-//   t  = sum_k |A(:,k)|^2 |B(k,:)|^2 4^{2044-ea-eb}  (E||AB||_F^2 for random signs).
+//   t  = sum_k |A(:,k)|^2 |B(k,:)|^2 4^{2044-ea-eb}  (E||AB||_F^2 for random signs),
+// and for the elementwise criterion the flattest row and column:
+//   ia = max_i 1 / A_i,  A_i = |a_i|^2 4^{1022-Er_i}  (rows with a_i = 0 left out),
+//   ib = max_j 1 / B_j,  B_j = |b_j|^2 4^{1022-Ec_j}.
+// A_i is the sum of the squared magnitudes of row i scaled by its own largest
+// element's power of two (each term < 1): about K/10 for a row of random
+// magnitudes, 1/4 or less for a row that one element dominates.
 struct KnobStats {
-    double sa, na, sb, nb, t;
+    double sa, na, sb, nb, t, ia, ib;
 };
+
+// Error criteria of the precision knob.
+enum KnobCriterion : int { KNOB_NORMWISE = 0, KNOB_ELEMENTWISE = 1 };
 
 // A-priori normwise relative error of the triangular pair set with s slices of
 // b bits.  Write x = 2^{E-1022} (sum_p x_p 2^{-b(p+1)} + r 2^{-bs}) with digits
@@ -103,12 +112,26 @@ struct KnobStats {
 // For phi <= 1 inputs the unscaled model is within a few percent of the
 // measured error; heavier tails make it conservative.  Non-finite or zero
 // statistics give an infinite estimate (the caller then takes its largest s).
-double knob_estimate(const KnobStats &k, int K, int b, int s);
+//
+// Elementwise criterion (crit = KNOB_ELEMENTWISE): the relative error of each
+// entry c_ij with |c_ij| >= tail h_ij, h_ij = |a_i| |b_j| / sqrt(K) the rms
+// scale of the entry's K terms.  Per entry the same first-order terms, summed
+// with random signs, give |e_ij| / h_ij = 2^{-bs} sqrt(K) sqrt(K (s-1)^2 /
+// (16 A_i B_j) + 1 / (3 A_i) + 1 / (3 B_j)) (h_ij = 2^{Er_i+Ec_j-2044}
+// sqrt(A_i B_j / K) exactly); the flattest row and column (ia, ib) bound it over
+// all entries:
+//   est_e(s) = 1.5 2^{-bs} sqrt(K) sqrt(K (s-1)^2 ia ib / 16 + (ia + ib) / 3) / tail + 2^{-53}.
+// No fixed precision bounds the relative error of an entry that cancels to
+// near zero; the tail leaves out the entries within tail h_ij of zero (about a
+// tail's fraction of them for random signs and phi <= 1; more for heavy tails,
+// whose few large terms make h_ij large against most entries).
+double knob_estimate(const KnobStats &k, int K, int b, int s, int crit = KNOB_NORMWISE, double tail = 1e-4);
 
-// Slice count for a requested normwise relative error: the smallest s in
-// [s_min, s_max] with knob_estimate <= bound (s_max if none).  Writes the
-// estimate for the returned s.
-int choose_slices_stats(const KnobStats &k, int K, int b, double bound, int s_min, int s_max, double *estimate);
+// Slice count for a requested relative error: the smallest s in [s_min, s_max]
+// with knob_estimate <= bound (s_max if none).  Writes the estimate for the
+// returned s.
+int choose_slices_stats(const KnobStats &k, int K, int b, double bound, int s_min, int s_max, double *estimate,
+                        int crit = KNOB_NORMWISE, double tail = 1e-4);
 
 // KnobStats computed on the host from stage-(a) style statistics.  ca/rb (the
 // per-k sums of squares of the columns of A and the rows of B) may be null:

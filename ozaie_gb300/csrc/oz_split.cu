@@ -12,6 +12,7 @@
 #include <cstdint>
 
 #include "oz_internal.h"
+#include "oz_plan.h"
 #include "oz_ptx.cuh"
 
 namespace ozgb {
@@ -323,6 +324,18 @@ __device__ int block_max_int(int v, int *sh) {
     return m;
 }
 
+__device__ double block_max_nonneg(double v, double *sh) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    double m = sh[0];
+    for (int w = 1; w < nw; ++w) m = fmax(m, sh[w]);
+    return m;
+}
+
 __device__ double block_sum(double v, double *sh) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
@@ -510,7 +523,10 @@ __device__ __forceinline__ void unit_sq_thread(const StatParts &sp, int u, int *
 // one warp per unit.  With ea, eb the largest row / column exponents of op(A) /
 // op(B):
 //   sa = sum_r 4^(Er - ea), na = sum_r |a_r|^2 4^(1022 - ea), likewise for B,
-//   t  = sum_k |op(A)(:,k)|^2 |op(B)(k,:)|^2 4^(2044 - ea - eb).
+//   t  = sum_k |op(A)(:,k)|^2 |op(B)(k,:)|^2 4^(2044 - ea - eb),
+// and for the elementwise criterion ia = max_r 1 / (|a_r|^2 4^(1022 - Er)) over
+// the non-zero rows (ib likewise over the columns of op(B)), combined by an
+// integer max of the bit patterns (order-preserving for non-negative doubles).
 __device__ __forceinline__ void knob_stats_body(const KnobJob &j, const int role, const int chunk, const int chunks) {
     __shared__ int sh_i[32];
     __shared__ double sh_d[32];
@@ -527,7 +543,11 @@ __device__ __forceinline__ void knob_stats_body(const KnobJob &j, const int role
     const int n = role == 0 ? j.M : (role == 1 ? j.N : j.K);
     const int per = (n + chunks - 1) / chunks;
     const int i0 = chunk * per, i1 = min(n, i0 + per);
-    double num = 0.0, den = 0.0, t = 0.0;
+    double num = 0.0, den = 0.0, t = 0.0, inv = 0.0;
+    // 1 / (|x_u|^2 4^(1022 - E_u)) of a unit whose squares sum to sq 4^(E - 1023)
+    auto flat_inv = [](float sq, int E, int Eu) {
+        return sq > 0.0f ? scale2(1.0 / static_cast<double>(sq), 2 * (Eu + 1 - E)) : 0.0;
+    };
     const int nparts = role == 0 ? j.ra.nparts : (role == 1 ? j.cb.nparts : max(j.ka.nparts, j.kb.nparts));
     if (nparts <= 32) {
         // one thread per unit
@@ -538,8 +558,10 @@ __device__ __forceinline__ void knob_stats_body(const KnobJob &j, const int role
                 int E;
                 float sq;
                 unit_sq_thread(sp, u, &E, &sq);
-                num += pow2i(2 * ((role == 0 ? j.er[u] : j.ec[u]) - emax));
+                const int Eu = role == 0 ? j.er[u] : j.ec[u];
+                num += pow2i(2 * (Eu - emax));
                 den += scale2(static_cast<double>(sq), 2 * (E - emax) - 2);
+                inv = fmax(inv, flat_inv(sq, E, Eu));
             } else {
                 int E1, E2;
                 float s1, s2;
@@ -558,8 +580,10 @@ __device__ __forceinline__ void knob_stats_body(const KnobJob &j, const int role
                 float sq;
                 unit_sq_warp(sp, u, lane, &E, &sq);
                 if (lane == 0) {
-                    num += pow2i(2 * ((role == 0 ? j.er[u] : j.ec[u]) - emax));
+                    const int Eu = role == 0 ? j.er[u] : j.ec[u];
+                    num += pow2i(2 * (Eu - emax));
                     den += scale2(static_cast<double>(sq), 2 * (E - emax) - 2);
+                    inv = fmax(inv, flat_inv(sq, E, Eu));
                 }
             } else {
                 int E1, E2;
@@ -573,9 +597,13 @@ __device__ __forceinline__ void knob_stats_body(const KnobJob &j, const int role
     if (role < 2) {
         num = block_sum(num, sh_d);
         den = block_sum(den, sh_d);
+        inv = block_max_nonneg(inv, sh_d);
         if (threadIdx.x == 0) {
             atomicAdd(j.out + 2 * role, num);
             atomicAdd(j.out + 2 * role + 1, den);
+            if (inv > 0.0)
+                atomicMax(reinterpret_cast<unsigned long long *>(j.out + 5 + role),
+                          static_cast<unsigned long long>(__double_as_longlong(inv)));
         }
     } else {
         t = block_sum(t, sh_d);
@@ -766,7 +794,7 @@ void launch_knob_grouped(const KnobJob *jobs, int n, void *stream) {
 void launch_knob_stats(const KnobJob &j, void *stream) {
     // each of the three sums split over blocks of 8 warps, about 64 units per block
     const int chunks = std::max(1, std::min(1024, std::max(j.M, std::max(j.N, j.K)) / 64));
-    cudaMemsetAsync(j.out, 0, 5 * sizeof(double), static_cast<cudaStream_t>(stream));
+    cudaMemsetAsync(j.out, 0, sizeof(KnobStats), static_cast<cudaStream_t>(stream));
     k_knob_stats<<<3 * chunks, 256, 0, static_cast<cudaStream_t>(stream)>>>(j);
 }
 

@@ -234,3 +234,52 @@ def test_plan_slice_format(ozlib, b, s, J):
         assert c["slice_format"] == 0 and c["k_chunk"] in (16, 32)
     max_pairs = max(_pairs(s, j + 1) - _pairs(s, j) for j in range(J))
     assert max_pairs * c["k_chunk"] * c["drain_chunks"] * (2 ** b - 1) ** 2 <= 2 ** 24
+
+
+def test_precision_knob_elementwise_formula(ozlib, oracle):
+    """The elementwise estimate against a direct evaluation of its model:
+    est(s) = 1.5 2^-bs sqrt(K) sqrt(K (s-1)^2 ia ib / 16 + (ia + ib) / 3) / tail + 2^-53,
+    ia = max_i 1 / (|a_i|^2 4^(1022 - Er_i)), ib likewise over the columns of B."""
+    K = 300
+    A = oracle.gen_phi((64, K), 3, 1.0)
+    B = oracle.gen_phi((K, 48), 4, 1.0)
+    er, ssr, ec, ssc, ca, rb = _stats(A, B)
+    ia = max(1.0 / (float(x) * 4.0 ** (1022 - int(e))) for x, e in zip(ssr, er))
+    ib = max(1.0 / (float(x) * 4.0 ** (1022 - int(e))) for x, e in zip(ssc, ec))
+    for tail in (1e-2, 1e-4):
+        def model(t):
+            r = K * (t - 1) ** 2 * ia * ib / 16 + (ia + ib) / 3
+            return 1.5 * 2.0 ** (-7 * t) * (K * r) ** 0.5 / tail + 2.0 ** -53
+
+        for bound in (1e-8, 1e-11, 1e-15):
+            s, est = ozlib.choose_slices(er, ssr, ec, ssc, K, 7, bound, ca, rb, criterion=1, tail=tail)
+            assert est == pytest.approx(model(s), rel=1e-9)
+            assert est <= bound and (s == 2 or model(s - 1) > bound)
+    # the elementwise criterion asks for at least as many slices as the normwise one
+    sn, _ = ozlib.choose_slices(er, ssr, ec, ssc, K, 7, 1e-13, ca, rb)
+    se, _ = ozlib.choose_slices(er, ssr, ec, ssc, K, 7, 1e-13, ca, rb, criterion=1, tail=1e-4)
+    assert se >= sn
+    assert ozlib.choose_slices(er, ssr, ec, ssc, K, 7, 1e-13, ca, rb, criterion=1, tail=0.0)[0] == -1
+
+
+@pytest.mark.parametrize("phi", [0.5, 1.0, 2.0, 4.0])
+def test_precision_knob_elementwise_meets_bound(ozlib, oracle, phi):
+    """With the elementwise criterion, every entry at least tail |a_i| |b_j| /
+    sqrt(K) away from zero meets the requested relative error against the exact
+    product (triangular pair set, RN)."""
+    tail = 1e-3
+    M, N, K = 96, 80, 700
+    A = oracle.gen_phi((M, K), 31, phi)
+    B = oracle.gen_phi((K, N), 32, phi)
+    er, ssr, ec, ssc, ca, rb = _stats(A, B)
+    rows = np.repeat(np.arange(M, dtype=np.int32), N)
+    cols = np.tile(np.arange(N, dtype=np.int32), M)
+    exact = oracle.exact_entries(A, B, rows, cols)[0].reshape(M, N)
+    scale = np.sqrt(np.outer(ssr, ssc) / K)
+    kept = np.abs(exact) >= tail * scale
+    assert kept.mean() > (0.99 if phi <= 2 else 0.8)
+    for bound in (1e-8, 1e-11, 1e-13, 1e-15):
+        s, _ = ozlib.choose_slices(er, ssr, ec, ssc, K, 7, bound, ca, rb, criterion=1, tail=tail)
+        C = oracle.dgemm(A, B, 7, s, s, 0)
+        rel = np.abs(C - exact)[kept] / np.abs(exact[kept])
+        assert rel.max() <= bound, (bound, s, rel.max())

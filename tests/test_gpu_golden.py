@@ -101,3 +101,24 @@ def test_device_knob_matches_host_knob(gpu_handle, oracle, ozlib, phi):
         assert (cfg["slices"], cfg["bins"]) == (s_host, s_host)
         ref = oracle.dgemm(A, B, 7, s_host, s_host, 0)
         assert np.array_equal(C.view(np.uint64), ref.view(np.uint64))
+
+
+@pytest.mark.parametrize("phi", [1.0, 4.0])
+def test_device_elementwise_knob_matches_host_knob(gpu_handle, oracle, ozlib, phi):
+    """The elementwise criterion on the device (flattest row and column from the
+    stage-(a) partial sums) picks the host knob's slice count."""
+    M, N, K = 300, 260, 1500
+    A = oracle.gen_phi((M, K), 33, phi)
+    B = oracle.gen_phi((K, N), 34, phi)
+    f = lambda x: ((x.view(np.uint64) >> np.uint64(52)) & np.uint64(0x7FF)).astype(np.int32)
+    gpu_handle.set_error_criterion(ozlib.Criterion.elementwise, 1e-3)
+    for bound in (1e-9, 1e-13):
+        s_host, _ = ozlib.choose_slices(f(A).max(axis=1), (A * A).sum(axis=1), f(B).max(axis=0), (B * B).sum(axis=0),
+                                        K, 7, bound, (A * A).sum(axis=0), (B * B).sum(axis=1), criterion=1,
+                                        tail=1e-3)
+        gpu_handle.set_error_bound(bound)
+        C = _dgemm(gpu_handle, A, B, 1)
+        cfg = gpu_handle.config()
+        assert (cfg["slices"], cfg["bins"]) == (s_host, s_host)
+        ref = oracle.dgemm(A, B, 7, s_host, s_host, 0)
+        assert np.array_equal(C.view(np.uint64), ref.view(np.uint64))
