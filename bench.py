@@ -12,8 +12,16 @@ Workload (one step = one full DGEMM through stages (a)-(d)):
 value : device-resident inputs (A, B in HBM before the timed region, 268 MB of
         inputs + 600 MB of slice planes per step, larger than the 126 MB L2),
         CUDA events on the launching stream, max over ranks.
+valid : the normwise relative error on 1000 sampled entries, against the exact
+        products and MPFR-106, is <= 1e-15 (accuracy_gate says why normwise);
+        the elementwise form of the bound is measured under elementwise_mode.
 e2e   : the reference-facing host-array call (ozAIE_DGEMM semantics) with host
-        copies in and out inside the timed region.
+        copies in and out inside the timed region, on pageable numpy arrays
+        (pinned arrays reported beside it).
+Also, by default: the batched workload (512 uneven problems, grouped vs per
+call), the long-K workload (8192 x 8192 x 65536 and its ill-conditioned
+variant), the accuracy-adaptive mix (65 problems up to 16384^3) and the 4096^3
+sweep (both pair sets, s = 3..8, phi in {0.5, 1, 2, 4}); --quick skips them.
 --impl reference : the reference's arithmetic on the host cores (the oracle port,
         OpenMP), bounded row sample of the same workload.
 """
@@ -210,31 +218,54 @@ def batched_run(n_probs, dev, stream, oz, O, torch):
         worst = max(worst, float(np.linalg.norm(got - ex) / max(np.linalg.norm(ex), 1e-300)))
     hg.close()
 
-    hp = oz.Handle()
-    hp.set_slices(8)
-    hp.set_bins(15)
+    def per_call(configure):
+        """Every problem through its own ozgb_dgemm_device call on one handle."""
+        hp = oz.Handle()
+        configure(hp)
 
-    def plain():
-        for pb in probs:
-            if hp.dgemm_device(pb["M"], pb["N"], pb["K"], pb["A"], pb["lda"], pb["B"], pb["ldb"], pb["C"], pb["ldc"],
-                               stream.cuda_stream):
-                raise RuntimeError(hp.last_error())
+        def run():
+            for pb in probs:
+                if hp.dgemm_device(pb["M"], pb["N"], pb["K"], pb["A"], pb["lda"], pb["B"], pb["ldb"], pb["C"],
+                                   pb["ldc"], stream.cuda_stream):
+                    raise RuntimeError(hp.last_error())
 
-    plain()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(2):
-        plain()
-    torch.cuda.synchronize()
-    p_ms = (time.perf_counter() - t0) / 2 * 1e3
-    hp.close()
+        run()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(2):
+            run()
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) / 2 * 1e3
+        if hp.sync():
+            raise RuntimeError(hp.last_error())
+        hp.close()
+        return ms
+
+    def fixed(s, J):
+        def f(h):
+            h.set_slices(s)
+            h.set_bins(J)
+        return f
+
+    # the grouped call's slice counts (all problems pick the same one here), run per call
+    s_used = int(np.bincount(np.asarray(used)).argmax())
+    p_ms = per_call(fixed(8, 15))                       # plain: the accurate configuration
+    a_ms = per_call(lambda h: h.set_error_bound(BOUND))  # per-call precision knob
+    e_ms = per_call(fixed(s_used, s_used))               # per-call, the grouped call's s and pair set
     return {"workload": "%d DGEMMs, M, N, K log-uniform in [32, 2048] (seed 7), phi=1, bound 1e-15 each" % n_probs,
             "effective_flop": flops,
             "grouped_adaptive_graph": {"value": flops / (g_ms * 1e-3) / 1e12, "unit": UNIT, "ms": g_ms,
                                        "slices_hist": {str(k): int(v) for k, v in
                                                        zip(*np.unique(used, return_counts=True))},
                                        "max_normwise_rel_err_sampled": worst},
+            "per_call_same_s_triangular": {"value": flops / (e_ms * 1e-3) / 1e12, "unit": UNIT, "ms": e_ms,
+                                           "slices": s_used, "bins": s_used},
+            "per_call_adaptive": {"value": flops / (a_ms * 1e-3) / 1e12, "unit": UNIT, "ms": a_ms},
             "plain_per_call_s8_full": {"value": flops / (p_ms * 1e-3) / 1e12, "unit": UNIT, "ms": p_ms},
+            "ratios": {
+                "grouping_at_equal_s_and_pairs": e_ms / g_ms,
+                "adaptive_vs_plain_per_call": p_ms / a_ms,
+                "grouped_adaptive_vs_plain_per_call": p_ms / g_ms},
             "speedup": p_ms / g_ms}
 
 
@@ -249,10 +280,14 @@ def device_phi(shape, seed, phi, dev, torch):
     return x
 
 
-def sampled_errors(dA, dB, dC, n, seed, O, torch):
+def sampled_errors(dA, dB, dC, n, seed, O, torch, tail=1e-4, mpfr=True):
     """Errors of n sampled entries of dC against the exact products (and MPFR-106
-    when libmpfr loads): only the sampled rows of A and columns of B leave the GPU."""
+    when libmpfr loads): only the sampled rows of A and columns of B leave the GPU.
+    max_rel is the largest elementwise relative error (the reference's reported
+    metric, common.h:585-592); max_rel_kept the same over the entries at least
+    tail |a_i| |b_j| / sqrt(K) away from zero (the elementwise criterion's set)."""
     M, N = dC.shape
+    K = dA.shape[1]
     r, c = O.sample_indices(M, N, n, seed)
     ri = torch.from_numpy(r.astype(np.int64)).to(dA.device)
     ci = torch.from_numpy(c.astype(np.int64)).to(dA.device)
@@ -260,13 +295,23 @@ def sampled_errors(dA, dB, dC, n, seed, O, torch):
     Bs = dB.index_select(1, ci).cpu().numpy()
     got = dC[ri, ci].cpu().numpy()
     idx = np.arange(n, dtype=np.int32)
-    ex, _ = O.exact_entries(As, Bs, idx, idx)
+    ex, absdot = O.exact_entries(As, Bs, idx, idx)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        rel = np.where(ex != 0, np.abs(got - ex) / np.abs(ex), np.where(got == ex, 0.0, np.inf))
+    scale = np.sqrt(np.sum(As * As, axis=1) * np.sum(Bs * Bs, axis=0) / K)
+    kept = np.abs(ex) >= tail * scale
     out = {"normwise_rel_vs_exact": float(np.linalg.norm(got - ex) / max(np.linalg.norm(ex), 1e-300)),
-           "max_rel_vs_exact": float(np.max(np.abs(got - ex) / np.maximum(np.abs(ex), 1e-300))),
+           "max_rel_vs_exact": float(np.max(rel)),
+           "max_rel_kept_vs_exact": float(np.max(rel[kept])) if kept.any() else 0.0,
+           "kept": int(kept.sum()),
+           "max_componentwise_vs_exact": float(np.max(np.abs(got - ex) / np.maximum(absdot, 1e-300))),
            "entries": n}
-    mp = O.mpfr_entries(As, Bs, idx, idx)
+    mp = O.mpfr_entries(As, Bs, idx, idx) if mpfr else None
     if mp is not None:
         out["normwise_rel_vs_mpfr106"] = float(np.linalg.norm(got - mp) / max(np.linalg.norm(mp), 1e-300))
+        with np.errstate(divide="ignore", invalid="ignore"):
+            relm = np.where(mp != 0, np.abs(got - mp) / np.abs(mp), np.where(got == mp, 0.0, np.inf))
+        out["max_rel_vs_mpfr106"] = float(np.max(relm))
     return out
 
 
@@ -339,27 +384,35 @@ def mix_sizes(n=64, seed=5, lo=1024, hi=16384):
 
 
 def mix_run(n, dev, stream, oz, O, torch):
-    """Per-problem calls over the mix: the precision knob (each problem's own
-    bound) against the plain accurate configuration (s = 8, full pair set) and
-    cuBLAS FP64, one problem resident at a time.  Errors are normwise over the
-    whole of C against a 16-slice Ozaki product (itself checked on sampled
-    entries against the exact products): with heavy-tailed entries (phi = 4) a
-    few large entries carry the norm of C, so a sampled normwise error says
-    little about the whole matrix."""
+    """Per-problem calls over the mix, one problem resident at a time: the
+    precision knob with each problem's own bound under both criteria (normwise,
+    and elementwise with tail 1e-4), the plain accurate configuration (s = 8,
+    full pair set) and cuBLAS FP64.  Every problem's results are checked on 256
+    sampled entries against the exact products (normwise and elementwise on the
+    samples); the normwise error over the whole of C is taken against a 16-slice
+    Ozaki product, itself checked on those samples against the exact products
+    (with heavy-tailed entries, phi = 4, a few large entries carry the norm of C,
+    so a sampled normwise error says little about the whole matrix)."""
     probs = mix_sizes(n)
 
-    def handle(slices=0, bins=0, bound=0.0):
+    def handle(slices=0, bins=0, bound=0.0, elementwise=False):
         h = oz.Handle()
         if slices:
             h.set_slices(slices)
             h.set_bins(bins)
         if bound:
             h.set_error_bound(bound)
+        if elementwise:
+            h.set_error_criterion(oz.Criterion.elementwise, 1e-4)
         return h
 
-    ha, hp, hr = handle(), handle(8, 15), handle(16, 16)  # knob; accurate mode's configuration; reference
-    tot = {"adaptive": 0.0, "plain_s8_full": 0.0, "cublas_dgemm": 0.0}
-    flops_all, met, worst_ratio, ref_worst, hist, per = 0.0, 0, 0.0, 0.0, {}, []
+    # knob (normwise); knob (elementwise); accurate mode's configuration; 16-slice reference
+    ha, he, hp, hr = handle(), handle(elementwise=True), handle(8, 15), handle(16, 16)
+    tot = {"adaptive": 0.0, "adaptive_elementwise": 0.0, "plain_s8_full": 0.0, "cublas_dgemm": 0.0}
+    flops_all, hist, hist_e, per = 0.0, {}, {}, []
+    met = {"normwise_all_vs_16_slices": 0, "normwise_sampled_vs_exact": 0, "elementwise_kept_sampled_vs_exact": 0}
+    worst = {"normwise_all_vs_16_slices": 0.0, "elementwise_kept_sampled_vs_exact": 0.0}
+    ref_worst = 0.0
     for i, (m, phi, bound) in enumerate(probs):
         dA = device_phi((m, m), 100 + i, phi, dev, torch)
         dB = device_phi((m, m), 200 + i, phi, dev, torch)
@@ -368,17 +421,24 @@ def mix_run(n, dev, stream, oz, O, torch):
         flops = 2.0 * m ** 3
         flops_all += flops
         ha.set_error_bound(bound)
+        he.set_error_bound(bound)
 
         def call(h, out):
             if h.dgemm_device(m, m, m, dA.data_ptr(), m, dB.data_ptr(), m, out.data_ptr(), m, stream.cuda_stream):
                 raise RuntimeError(h.last_error())
 
         call(hr, dR)
-        ref_worst = max(ref_worst, sampled_errors(dA, dB, dR, 64, i, O, torch)["normwise_rel_vs_exact"])
+        ref_worst = max(ref_worst, sampled_errors(dA, dB, dR, 64, i, O, torch, mpfr=False)["normwise_rel_vs_exact"])
         rn = torch.linalg.norm(dR).item()
         call(hp, dC)
         tp = time_device(lambda: call(hp, dC), torch, stream)
         ep = torch.linalg.norm(dC - dR).item() / rn
+        call(he, dC)
+        te = time_device(lambda: call(he, dC), torch, stream)
+        if he.sync():
+            raise RuntimeError(he.last_error())
+        se = he.config()["slices"]
+        ee = sampled_errors(dA, dB, dC, 256, 1000 + i, O, torch, mpfr=False)
         call(ha, dC)
         ta = time_device(lambda: call(ha, dC), torch, stream)
         for h in (ha, hp, hr):
@@ -386,33 +446,48 @@ def mix_run(n, dev, stream, oz, O, torch):
                 raise RuntimeError(h.last_error())
         s = ha.config()["slices"]
         ea = torch.linalg.norm(dC - dR).item() / rn
+        sa = sampled_errors(dA, dB, dC, 256, 1000 + i, O, torch, mpfr=False)
         tc = time_device(lambda: torch.matmul(dA, dB, out=dC), torch, stream)
         ec = torch.linalg.norm(dC - dR).item() / rn
         tot["adaptive"] += ta
+        tot["adaptive_elementwise"] += te
         tot["plain_s8_full"] += tp
         tot["cublas_dgemm"] += tc
-        met += int(ea <= bound)
-        worst_ratio = max(worst_ratio, ea / bound)
+        met["normwise_all_vs_16_slices"] += int(ea <= bound)
+        met["normwise_sampled_vs_exact"] += int(sa["normwise_rel_vs_exact"] <= bound)
+        met["elementwise_kept_sampled_vs_exact"] += int(ee["max_rel_kept_vs_exact"] <= bound)
+        worst["normwise_all_vs_16_slices"] = max(worst["normwise_all_vs_16_slices"], ea / bound)
+        worst["elementwise_kept_sampled_vs_exact"] = max(worst["elementwise_kept_sampled_vs_exact"],
+                                                         ee["max_rel_kept_vs_exact"] / bound)
         hist[str(s)] = hist.get(str(s), 0) + 1
-        per.append([m, phi, bound, s, round(ta, 3), round(tp, 3), round(tc, 3), ea, ep, ec])
+        hist_e[str(se)] = hist_e.get(str(se), 0) + 1
+        per.append([m, phi, bound, s, se, round(ta, 3), round(te, 3), round(tp, 3), round(tc, 3), ea,
+                    sa["normwise_rel_vs_exact"], sa["max_rel_vs_exact"], ee["max_rel_kept_vs_exact"], ep, ec])
         del dA, dB, dR, dC
-    for h in (ha, hp, hr):
+    for h in (ha, he, hp, hr):
         h.close()
     return {"workload": "%d square DGEMMs, size log-uniform in [1024, 16384] (seed 5), plus one 16384^3; "
                         "phi from {0.5, 1, 2, 4}, bound from {1e-8, 1e-11, 1e-13, 1e-15} per problem; "
                         "device-drawn operands" % n,
             "effective_flop": flops_all,
-            "error_reference": {"what": "Ozaki, 16 slices, triangular pair set, normwise over all of C",
-                                "its_worst_sampled_normwise_vs_exact": ref_worst},
+            "error_reference": {"sampled": "exact products on 256 sampled entries of every problem",
+                                "whole_matrix": "Ozaki, 16 slices, triangular pair set, normwise over all of C",
+                                "whole_matrix_reference_worst_sampled_normwise_vs_exact": ref_worst},
+            "bounds_met": met, "problems": len(probs), "worst_err_over_bound": worst,
             "adaptive": {"value": flops_all / (tot["adaptive"] * 1e-3) / 1e12, "unit": UNIT, "ms": tot["adaptive"],
-                         "slices_hist": hist, "bounds_met": met, "problems": len(probs),
-                         "worst_err_over_bound": worst_ratio},
+                         "criterion": "normwise", "slices_hist": hist},
+            "adaptive_elementwise": {"value": flops_all / (tot["adaptive_elementwise"] * 1e-3) / 1e12, "unit": UNIT,
+                                     "ms": tot["adaptive_elementwise"], "criterion": "elementwise, tail 1e-4",
+                                     "slices_hist": hist_e},
             "plain_s8_full": {"value": flops_all / (tot["plain_s8_full"] * 1e-3) / 1e12, "unit": UNIT,
                               "ms": tot["plain_s8_full"]},
             "cublas_dgemm": {"value": flops_all / (tot["cublas_dgemm"] * 1e-3) / 1e12, "unit": UNIT,
                              "ms": tot["cublas_dgemm"]},
-            "per_problem": {"columns": ["n", "phi", "bound", "slices", "adaptive_ms", "plain_ms", "cublas_ms",
-                                        "adaptive_err", "plain_err", "cublas_err"], "rows": per}}
+            "per_problem": {"columns": ["n", "phi", "bound", "slices", "slices_elementwise", "adaptive_ms",
+                                        "elementwise_ms", "plain_ms", "cublas_ms", "adaptive_err_all_vs_16",
+                                        "adaptive_err_sampled_normwise", "adaptive_err_sampled_max_rel",
+                                        "elementwise_err_sampled_max_rel_kept", "plain_err_all_vs_16",
+                                        "cublas_err_all_vs_16"], "rows": per}}
 
 
 def sweep_run(dev, stream, oz, O, torch):
@@ -443,9 +518,11 @@ def sweep_run(dev, stream, oz, O, torch):
         def errs(C):
             got = C[r, c]
             e = {"sampled_normwise_vs_exact": float(np.linalg.norm(got - exact) / np.linalg.norm(exact)),
+                 "sampled_max_rel_vs_exact": float(np.max(np.abs(got - exact) / np.maximum(np.abs(exact), 1e-300))),
                  "sampled_max_componentwise": float(np.max(np.abs(got - exact) / np.maximum(absdot, 1e-300)))}
             if mp is not None:
                 e["sampled_normwise_vs_mpfr106"] = float(np.linalg.norm(got - mp) / np.linalg.norm(mp))
+                e["sampled_max_rel_vs_mpfr106"] = float(np.max(np.abs(got - mp) / np.maximum(np.abs(mp), 1e-300)))
             return e
 
         ms = time_device(lambda: torch.matmul(dA, dB, out=dC), torch, stream, 1)
@@ -519,13 +596,16 @@ def main():
     ap.add_argument("--slices", type=int, default=0, help="fixed triangular slice count for --profile-only")
     ap.add_argument("--batched", type=int, default=512, help="problems in the batched comparison (0: skip)")
     ap.add_argument("--no-autotune", action="store_true", help="use the planner's cost-model plans")
-    ap.add_argument("--longk", action="store_true", help="add the long-K workload (8192^2 x 65536, ~1 min)")
-    ap.add_argument("--mix", type=int, default=0, help="add the accuracy-adaptive mix of this many problems")
-    ap.add_argument("--sweep", action="store_true",
-                    help="add the 4096^3 grid: both pair sets, s = 3..8, phi in {0.5, 1, 2, 4} (~1 min)")
+    ap.add_argument("--no-longk", action="store_true", help="skip the long-K workload (8192^2 x 65536)")
+    ap.add_argument("--mix", type=int, default=64, help="problems of the accuracy-adaptive mix (0: skip)")
+    ap.add_argument("--no-sweep", action="store_true",
+                    help="skip the 4096^3 grid: both pair sets, s = 3..8, phi in {0.5, 1, 2, 4}")
+    ap.add_argument("--quick", action="store_true", help="headline only: no batched, long-K, mix or sweep runs")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.quick:
+        args.batched, args.mix, args.no_longk, args.no_sweep = 0, 0, True, True
     if args.impl == "reference":
         return run_reference(args)
 
@@ -556,7 +636,7 @@ def main():
     if not args.no_autotune:
         # the precision knob picks s = 9 for this workload: tune that plan (and its
         # neighbours) before anything is timed
-        tuned = {str(s): h.autotune(M, N, K, 7, s, s, max_candidates=24) for s in (8, 9, 10)}
+        tuned = {str(s): h.autotune(M, N, K, 7, s, s, max_candidates=24) for s in (8, 9, 10, 11, 12)}
     h.set_error_bound(BOUND)
     if args.profile_only and args.slices:
         h.set_slices(args.slices)
@@ -644,22 +724,54 @@ def main():
     flops = 2.0 * M * N * K
     value = flops * ws / (ms * 1e-3) / 1e12
 
-    # e2e: host arrays through the reference-facing call, copies inside the timed region
-    # inputs and result in pinned host memory, as a caller streaming many products would keep them
-    A_host = torch.from_numpy(A).pin_memory().numpy()
-    B_host = torch.from_numpy(B).pin_memory().numpy()
-    he = oz.Handle()
-    he.set_error_bound(BOUND)
-    assert he.setup(M, N, K, oz.Mode.fast) == 0, he.last_error()
-    Ch = torch.empty((M, N), dtype=torch.float64).pin_memory().numpy()
-    for _ in range(2):
-        assert he.dgemm(M, N, K, A_host, B_host, Ch) == 0, he.last_error()
+    # e2e: host arrays through the reference-facing call (ozAIE_DGEMM semantics),
+    # copies in and out inside the timed region.  Primary: plain pageable numpy
+    # arrays, as the reference's own caller passes std::vector memory
+    # (example/oztest.cpp); also pinned arrays, as a caller streaming many products
+    # would keep them.
     e2e_steps = max(3, min(args.steps, 10))
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        assert he.dgemm(M, N, K, A_host, B_host, Ch) == 0, he.last_error()
-    e2e_ms = (time.perf_counter() - t0) / e2e_steps * 1e3
-    he.close()
+
+    def e2e_time(Ah, Bh, Ch):
+        he = oz.Handle()
+        he.set_error_bound(BOUND)
+        assert he.setup(M, N, K, oz.Mode.fast) == 0, he.last_error()
+        for _ in range(2):
+            assert he.dgemm(M, N, K, Ah, Bh, Ch) == 0, he.last_error()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            assert he.dgemm(M, N, K, Ah, Bh, Ch) == 0, he.last_error()
+        t = (time.perf_counter() - t0) / e2e_steps * 1e3
+        he.close()
+        return t
+
+    e2e_ms = e2e_time(np.ascontiguousarray(A), np.ascontiguousarray(B), np.empty((M, N)))
+    e2e_pinned_ms = e2e_time(torch.from_numpy(A).pin_memory().numpy(), torch.from_numpy(B).pin_memory().numpy(),
+                             torch.empty((M, N), dtype=torch.float64).pin_memory().numpy())
+
+    # the same product with the knob's elementwise criterion: relative error of
+    # every entry at least 1e-4 |a_i| |b_j| / sqrt(K) away from zero <= 1e-15
+    hq = oz.Handle()
+    hq.set_error_bound(BOUND)
+    hq.set_error_criterion(oz.Criterion.elementwise, 1e-4)
+
+    def step_e():
+        if hq.dgemm_device(M, N, K, dA.data_ptr(), K, dB.data_ptr(), N, dC.data_ptr(), N, stream.cuda_stream):
+            raise RuntimeError(hq.last_error())
+
+    for _ in range(3):
+        step_e()
+    el_ms = time_device(step_e, torch, stream, max(3, min(args.steps, 20)))
+    if hq.sync():
+        raise RuntimeError(hq.last_error())
+    el_cfg = hq.config()
+    hq.close()
+    el_err = sampled_errors(dA, dB, dC, 1000, 3, O, torch) if rank == 0 else None
+    elementwise_mode = {
+        "value": 2.0 * M * N * K / (el_ms * 1e-3) / 1e12, "unit": UNIT, "ms_per_step": el_ms,
+        "criterion": "elementwise relative error <= 1e-15 for every entry with |c_ij| >= 1e-4 |a_i| |b_j| / sqrt(K)",
+        "slices": el_cfg["slices"], "bins": el_cfg["bins"], "pairs": el_cfg["pairs"], "accuracy": el_err,
+        "valid_elementwise_all_sampled_vs_mpfr106": bool(el_err and el_err.get("max_rel_vs_mpfr106", 1.0) <= BOUND),
+        "valid_elementwise_kept_sampled_vs_exact": bool(el_err and el_err["max_rel_kept_vs_exact"] <= BOUND)}
 
     # native FP64 DGEMM (cuBLAS through torch) on the same GPU, and its accuracy
     for _ in range(2):
@@ -676,9 +788,9 @@ def main():
     err_cublas = O.error_report(dC.cpu().numpy(), A, B, r, c, exact, absdot)
 
     batched = batched_run(args.batched, dev, stream, oz, O, torch) if args.batched > 0 and rank == 0 else None
-    long_k = long_k_run(dev, stream, oz, O, torch) if args.longk and rank == 0 else None
+    long_k = long_k_run(dev, stream, oz, O, torch) if not args.no_longk and rank == 0 else None
     mix = mix_run(args.mix, dev, stream, oz, O, torch) if args.mix > 0 and rank == 0 else None
-    sweep = sweep_run(dev, stream, oz, O, torch) if args.sweep and rank == 0 else None
+    sweep = sweep_run(dev, stream, oz, O, torch) if not args.no_sweep and rank == 0 else None
 
     peaks = load_peaks()
     mma_flops = 2.0 * cfg["pairs"] * M * N * K
@@ -697,12 +809,24 @@ def main():
                        "tile_n": cfg["tile_n"], "k_chunk": cfg["k_chunk"], "stages": cfg["stages"],
                        "l2": "inputs + slice planes (~870 MB) larger than L2 (126 MB); no flush needed",
                        "parallelism": "weak: one independent DGEMM per GPU" if ws > 1 else "single GPU"},
-            "valid": bool(err["normwise_rel"] <= BOUND),
+            "valid": bool(err["normwise_rel"] <= BOUND and (err_mpfr is None or err_mpfr["normwise_rel"] <= BOUND)),
+            "accuracy_gate": {
+                "bound": BOUND,
+                "applies_to": "normwise relative error |C^ - C|_F / |C|_F on 1000 sampled entries, against the "
+                              "exact products and against MPFR-106",
+                "why_not_elementwise": "the largest elementwise relative error is set by entries that cancel to "
+                                       "near zero: native FP64 DGEMM (cublas_dgemm_vs_exact.max_rel) misses 1e-15 by "
+                                       "three orders of magnitude on these inputs; the elementwise form of the "
+                                       "bound is reported under elementwise_mode"},
             "accuracy": {"vs_exact": err, "vs_mpfr106": err_mpfr, "cublas_dgemm_vs_exact": err_cublas},
+            "elementwise_mode": elementwise_mode,
             "stage_ms": {k: statistics.median([t[k] for t in stage]) for k in stage[0]},
             "cublas_dgemm": {"value": flops / (cublas_ms * 1e-3) / 1e12, "unit": UNIT, "ms": cublas_ms},
             "e2e": {"value": flops / (e2e_ms * 1e-3) / 1e12, "unit": UNIT, "ms_per_step": e2e_ms,
-                    "h2d_bytes_per_step": 2 * M * K * 8, "d2h_bytes_per_step": M * N * 8},
+                    "host_memory": "pageable (plain numpy arrays)",
+                    "h2d_bytes_per_step": 2 * M * K * 8, "d2h_bytes_per_step": M * N * 8,
+                    "pinned": {"value": flops / (e2e_pinned_ms * 1e-3) / 1e12, "unit": UNIT,
+                               "ms_per_step": e2e_pinned_ms}},
             "roofline": {"bound": "tensor", "kernel": "oz_gemm_kernel (slice-pair GEMM + exact drain + decode)",
                          "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                          "frac": achieved / peaks["bf16_tflops"], "traffic": traffic,

@@ -502,11 +502,9 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
         if ((rc = set_tail_split(h, p, 0, t_split, st, &g))) return rc;
         p.fn(g, t_split, p.smem, st);
         cudaEventRecord(h->ev_part, st);
-        cudaStreamWaitEvent(h->aux[0], h->ev_part, 0);
-        const size_t n1 = static_cast<size_t>(rows_split) * o.N;
-        if ((e = cudaMemcpyAsync(ho->C, o.C, n1 * 8, cudaMemcpyDeviceToHost, h->aux[0])) != cudaSuccess)
-            return cuda_fail(h, e, "copy C (first rows)");
-        cudaEventRecord(h->ev_part_copied, h->aux[0]);
+        // both launches are enqueued before the first copy: a copy into pageable
+        // host memory returns only when it has completed, which would otherwise
+        // hold the second launch back until the first part is done and copied
         if ((rc = set_tail_split(h, p, t_split, total, st, &g))) return rc;
         p.fn(g, total - t_split, p.smem, st);
         h->launches += 2;
@@ -515,6 +513,11 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
             cudaEventRecord(h->ev[3], st);
             h->ev_recorded = true;
         }
+        cudaStreamWaitEvent(h->aux[0], h->ev_part, 0);
+        const size_t n1 = static_cast<size_t>(rows_split) * o.N;
+        if ((e = cudaMemcpyAsync(ho->C, o.C, n1 * 8, cudaMemcpyDeviceToHost, h->aux[0])) != cudaSuccess)
+            return cuda_fail(h, e, "copy C (first rows)");
+        cudaEventRecord(h->ev_part_copied, h->aux[0]);
         const size_t n2 = static_cast<size_t>(o.M - rows_split) * o.N;
         if ((e = cudaMemcpyAsync(ho->C + n1, o.C + n1, n2 * 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
             return cuda_fail(h, e, "copy C (last rows)");
