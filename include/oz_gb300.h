@@ -186,6 +186,11 @@ ozgb_status ozgb_set_error_bound(ozgb_handle h, double bound);
 enum { OZGB_CRIT_NORMWISE = 0, OZGB_CRIT_ELEMENTWISE = 1 };
 ozgb_status ozgb_set_error_criterion(ozgb_handle h, int criterion, double tail);
 ozgb_status ozgb_set_graph(ozgb_handle h, int enable);     /* capture grouped calls in CUDA graphs */
+/* Grouped calls' slice-pair GEMMs: 1 (default) = one persistent launch per plan
+ * class (the problems whose plans share the kernel variant, stage layout, bin
+ * blocks, drain schedule and accumulator groups), its CTAs walking the tiles of
+ * all of its problems, largest problems first; 0 = one launch per problem. */
+ozgb_status ozgb_set_grouped_launch(ozgb_handle h, int mode);
 ozgb_status ozgb_set_timeout_ms(ozgb_handle h, double ms); /* device-side wait limit, default 2000 */
 ozgb_status ozgb_get_config(ozgb_handle h, ozgb_config *out);
 /* Per-stage device times of the last call (ms): [0] exponents, [1] split,
@@ -257,6 +262,17 @@ int ozgb_choose_slices(const int32_t *er, const double *ssr, int M, const int32_
 int ozgb_choose_slices_ex(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N,
                           const double *sa_k, const double *sb_k, int K, int bits, double bound, int criterion,
                           double tail, double *estimate);
+
+/* Host-only check of the grouped launches (no device needed, a test hook): the
+ * launches that ozgb_dgemm_grouped would make for these problems (b = 7,
+ * `slices`, `bins`, round to nearest; A, B unused; C pointers and ldc as given)
+ * are built with stand-in device addresses, and every work unit is walked as the
+ * kernel walks it: each tile of each problem exactly once, every bulk copy inside
+ * the problem's slice blocks, the epilogue's C and exponents those of its
+ * problem.  Returns 0 and the number of launches and work units, or a negative
+ * code naming the first violated check. */
+int ozgb_grouped_layout_check(const ozgb_problem *probs, int n, int slices, int bins, int *launches_out,
+                              long long *units_out);
 
 /* Library version string. */
 const char *ozgb_version(void);

@@ -81,6 +81,9 @@ SIGNATURES = [
     ("ozgb_set_error_bound", _i, [_h, _dbl]),
     ("ozgb_set_error_criterion", _i, [_h, _i, _dbl]),
     ("ozgb_set_graph", _i, [_h, _i]),
+    ("ozgb_set_grouped_launch", _i, [_h, _i]),
+    ("ozgb_grouped_layout_check", _i, [ctypes.POINTER(OzgbProblem), _i, _i, _i, ctypes.POINTER(_i),
+                                       ctypes.POINTER(ctypes.c_longlong)]),
     ("ozgb_set_timeout_ms", _i, [_h, _dbl]),
     ("ozgb_get_config", _i, [_h, ctypes.POINTER(OzgbConfig)]),
     ("ozgb_set_profiling", _i, [_h, _i]),

@@ -153,6 +153,10 @@ class Handle:
     def set_graph(self, on):
         return self._check(self._L.ozgb_set_graph(self._h, 1 if on else 0))
 
+    def set_grouped_launch(self, mode):
+        """1: one persistent GEMM launch per plan class (default); 0: one per problem."""
+        return self._check(self._L.ozgb_set_grouped_launch(self._h, int(mode)))
+
     def set_timeout_ms(self, ms):
         return self._check(self._L.ozgb_set_timeout_ms(self._h, float(ms)))
 
@@ -240,6 +244,20 @@ def tuning_entries():
 
 def tuning_clear():
     load().ozgb_tuning_clear()
+
+
+def grouped_layout_check(sizes, slices, bins=0):
+    """Host-only walk of the grouped launches for problems of the given (M, N, K)
+    sizes: (status, launches, work units); status 0 when every check holds."""
+    arr = (OzgbProblem * len(sizes))()
+    base = 1 << 42
+    for i, (M, N, K) in enumerate(sizes):
+        arr[i] = OzgbProblem(int(M), int(N), int(K), None, int(K), None, int(N), base, int(N), 0.0, 0)
+        base += ((int(M) * int(N) * 8 + 255) // 256) * 256
+    nl = ctypes.c_int()
+    nu = ctypes.c_longlong()
+    rc = load().ozgb_grouped_layout_check(arr, len(sizes), int(slices), int(bins), ctypes.byref(nl), ctypes.byref(nu))
+    return rc, nl.value, nu.value
 
 
 def plan_query(M, N, K, bits, slices, bins):

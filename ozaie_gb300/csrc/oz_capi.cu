@@ -14,11 +14,13 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
 
 #include "oz_gb300.h"
+#include "oz_gemm.cuh"
 #include "oz_internal.h"
 #include "oz_plan.h"
 
@@ -76,6 +78,8 @@ struct ozgb_context {
     bool split_dirty = true;
     KnobJob kjob{};  // the last stage-(a) statistics, for the precision knob
     DevBuf gstat, gslice, gtab;  // grouped calls: statistics, slice planes, job/problem tables
+    DevBuf gprob;                // grouped calls: per-launch problem tables of the slice-pair GEMMs
+    int grouped_launch = 1;      // 1: one persistent GEMM launch per plan class; 0: one per problem
     cudaStream_t stream = nullptr;       // used by the host-array entry points
     // grouped calls: the per-problem GEMMs run on auxiliary streams forked from
     // and joined back into the caller's stream
@@ -664,6 +668,85 @@ ozgb_status run_phase(ozgb_handle h, bool graph, const std::vector<long long> &k
     return e == cudaSuccess ? OZGB_OK : cuda_fail(h, e, "graph launch");
 }
 
+// One grouped slice-pair GEMM launch: the problems whose plans share the kernel
+// variant and every launch-level GemmArgs field (stage layout, bin blocks, drain
+// schedule, accumulator groups, rounding).  Its work units are the tiles of its
+// problems, largest problems first, so that small problems fill the last waves.
+struct GroupLaunch {
+    GemmArgs g;         // launch-level fields (probs / tile_prob set when uploaded)
+    const Plan *plan;   // the plan of its first problem: variant and shared memory
+    std::vector<GroupProblem> probs;
+    std::vector<int> tile_prob;
+    double cost = 0.0;  // tiles x chunks x pairs
+};
+
+std::vector<long long> launch_key(const GemmArgs &g, const Plan &p) {
+    std::vector<long long> k = {reinterpret_cast<long long>(p.fn), static_cast<long long>(p.smem), g.KC, g.s, g.J,
+                                g.b, g.out_mode, g.stages, g.stage_bytes, g.a_block_bytes, g.b_block_bytes,
+                                g.b_pad_lo_bytes, g.b_region_bytes, g.tmem_cols, g.n_acc, g.n_iss, g.G};
+    for (int a = 0; a < kMaxAcc; ++a) k.push_back(g.acc_t0[a]);
+    for (int i = 0; i < g.G; ++i)
+        k.insert(k.end(), {g.blk_lo[i], g.blk_nb[i], g.blk_p0[i], g.blk_p1[i], g.blk_period[i], g.blk_off[i]});
+    return k;
+}
+
+// The grouped launches of n problems with the given plans and device addresses
+// of their slice blocks and exponents.
+std::vector<GroupLaunch> build_group_launches(const ozgb_problem *probs, int n, const std::vector<Plan> &plans,
+                                              const std::vector<const uint8_t *> &a_tiles,
+                                              const std::vector<const uint8_t *> &b_tiles,
+                                              const std::vector<const int32_t *> &er,
+                                              const std::vector<const int32_t *> &ec, int *err,
+                                              unsigned long long timeout_ns) {
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    auto cost = [&](int i) {
+        return static_cast<double>(plans[i].tiles_m) * plans[i].tiles_n * plans[i].n_kc * plans[i].pairs;
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost(x) > cost(y); });
+    std::vector<GroupLaunch> out;
+    std::map<std::vector<long long>, size_t> index;
+    for (int i : order) {
+        const Plan &p = plans[i];
+        GemmArgs g;
+        gemm_args_from_plan(&g, p, p.cfg.rounding, err, timeout_ns);
+        const std::vector<long long> key = launch_key(g, p);
+        auto it = index.find(key);
+        if (it == index.end()) {
+            it = index.emplace(key, out.size()).first;
+            out.emplace_back();
+            out.back().g = g;
+            out.back().plan = &p;
+        }
+        GroupLaunch &L = out[it->second];
+        GroupProblem gp{};
+        gp.a_tiles = a_tiles[i];
+        gp.b_tiles = b_tiles[i];
+        gp.er = er[i];
+        gp.ec = ec[i];
+        gp.c = probs[i].C;
+        gp.ldc = probs[i].ldc;
+        gp.M = probs[i].M;
+        gp.N = probs[i].N;
+        gp.n_kc = p.n_kc;
+        gp.tiles_m = p.tiles_m;
+        gp.tiles_n = p.tiles_n;
+        gp.tile0 = static_cast<int>(L.tile_prob.size());
+        const int idx = static_cast<int>(L.probs.size());
+        L.probs.push_back(gp);
+        L.tile_prob.insert(L.tile_prob.end(), static_cast<size_t>(p.tiles_m) * p.tiles_n, idx);
+        L.cost += cost(i);
+    }
+    for (GroupLaunch &L : out) {
+        L.g.tile_begin = 0;
+        L.g.total_tiles = static_cast<int>(L.tile_prob.size());
+        L.g.split_parts = 1;  // no K-split: the problems side by side fill the SMs
+        L.g.split_start = L.g.total_tiles;
+    }
+    std::stable_sort(out.begin(), out.end(), [](const GroupLaunch &x, const GroupLaunch &y) { return x.cost > y.cost; });
+    return out;
+}
+
 // The grouped pipeline: one launch for every problem's stage (a) (and the knob's
 // statistics), one grouped knob reduction and a single read-back when any
 // problem asks for an error bound, one launch for every problem's split, and the
@@ -672,6 +755,12 @@ ozgb_status run_phase(ozgb_handle h, bool graph, const std::vector<long long> &k
 // stay the same.
 ozgb_status enqueue_grouped(ozgb_handle h, ozgb_problem *probs, int n, int mode, cudaStream_t st) {
     const bool graph = h->use_graph != 0;
+    // a call without graphs rewrites the job and problem tables that captured
+    // graphs read: those graphs may not be replayed afterwards
+    if (!graph) {
+        h->gkey1.clear();
+        h->gkey2.clear();
+    }
     const bool prof = h->profiling && !graph;
     std::vector<double> bound(n, 0.0);
     std::vector<int> adapt_idx(n, -1);
@@ -836,7 +925,48 @@ ozgb_status enqueue_grouped(ozgb_handle h, ozgb_problem *probs, int n, int mode,
         key2.insert(key2.end(), {reinterpret_cast<long long>(probs[i].C), probs[i].ldc, p.cfg.b, p.cfg.s, p.cfg.J,
                                  p.cfg.rounding, p.BN, p.KC, p.stages, p.G});
     }
+    // grouped GEMM launches (one per plan class) and their problem tables; the
+    // tables are uploaded unless the captured graph of the same calls is replayed
+    std::vector<GroupLaunch> launches;
+    if (h->grouped_launch) {
+        std::vector<const uint8_t *> a_t(n), b_t(n);
+        std::vector<const int32_t *> e_r(n), e_c(n);
+        for (int i = 0; i < n; ++i) {
+            a_t[i] = gsl + a_off[i];
+            b_t[i] = gsl + b_off[i];
+            e_r[i] = reinterpret_cast<const int32_t *>(at(so[i].er));
+            e_c[i] = reinterpret_cast<const int32_t *>(at(so[i].ec));
+        }
+        launches = build_group_launches(probs, n, plans, a_t, b_t, e_r, e_c, static_cast<int *>(h->err.p),
+                                        h->timeout_ns);
+        size_t bytes = 0;
+        for (const GroupLaunch &L : launches)
+            bytes += align256(sizeof(GroupProblem) * L.probs.size()) + align256(sizeof(int) * L.tile_prob.size());
+        if (!h->gprob.ensure(bytes)) return fail(h, OZGB_ERR_ALLOC, "grouped problem tables");
+        uint8_t *base = static_cast<uint8_t *>(h->gprob.p);
+        size_t off = 0;
+        for (GroupLaunch &L : launches) {
+            L.g.probs = reinterpret_cast<GroupProblem *>(base + off);
+            off += align256(sizeof(GroupProblem) * L.probs.size());
+            L.g.tile_prob = reinterpret_cast<int *>(base + off);
+            off += align256(sizeof(int) * L.tile_prob.size());
+            const std::vector<long long> lk = launch_key(L.g, *L.plan);
+            key2.insert(key2.end(), lk.begin(), lk.end());
+            key2.insert(key2.end(), {reinterpret_cast<long long>(L.g.probs), static_cast<long long>(L.probs.size())});
+        }
+    }
+    key2.push_back(h->grouped_launch);
     const bool replay2 = graph && h->gexec2 && h->gkey2 == key2;
+    if (h->grouped_launch && !replay2) {
+        for (GroupLaunch &L : launches) {
+            const cudaError_t e1 = cudaMemcpyAsync(const_cast<GroupProblem *>(L.g.probs), L.probs.data(),
+                                                   sizeof(GroupProblem) * L.probs.size(), cudaMemcpyHostToDevice, st);
+            const cudaError_t e2 = cudaMemcpyAsync(const_cast<int *>(L.g.tile_prob), L.tile_prob.data(),
+                                                   sizeof(int) * L.tile_prob.size(), cudaMemcpyHostToDevice, st);
+            if (e1 != cudaSuccess || e2 != cudaSuccess)
+                return cuda_fail(h, e1 != cudaSuccess ? e1 : e2, "grouped problem table upload");
+        }
+    }
     JobList jb;
     for (int i = 0; i < n; ++i) {
         const ozgb_problem &pb = probs[i];
@@ -862,20 +992,26 @@ ozgb_status enqueue_grouped(ozgb_handle h, ozgb_problem *probs, int n, int mode,
         djb = put_table(h, jb.jobs, &toff, st);
         dbb = put_table(h, jb.block0, &toff, st);
     }
-    // the GEMMs, largest first, spread over the auxiliary streams
+    // the GEMMs: one persistent launch per plan class (grouped_launch), or one per
+    // problem, largest first, spread over the auxiliary streams
     std::vector<int> order(n);
     for (int i = 0; i < n; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
         return static_cast<double>(plans[x].tiles_m) * plans[x].tiles_n * plans[x].n_kc * plans[x].pairs >
                static_cast<double>(plans[y].tiles_m) * plans[y].tiles_n * plans[y].n_kc * plans[y].pairs;
     });
-    const int n_aux = std::min(n, static_cast<int>(ozgb_context::kAux));
+    const int n_streams = h->grouped_launch ? static_cast<int>(launches.size()) : n;
+    const int n_aux = std::max(1, std::min(n_streams, static_cast<int>(ozgb_context::kAux)));
     rc = run_phase(h, graph, key2, &h->gkey2, &h->gexec2, st, [&](cudaStream_t s) -> ozgb_status {
         launch_stage_jobs(djb, dbb, static_cast<int>(jb.jobs.size()), jb.total, s);
         if (prof) cudaEventRecord(h->ev[2], s);
         cudaEventRecord(h->ev_fork, s);
         for (int a = 0; a < n_aux; ++a) cudaStreamWaitEvent(h->aux[a], h->ev_fork, 0);
-        for (int r = 0; r < n; ++r) {
+        for (size_t l = 0; l < launches.size(); ++l) {
+            const GroupLaunch &L = launches[l];
+            L.plan->fn(L.g, L.g.total_tiles, L.plan->smem, h->aux[l % n_aux]);
+        }
+        for (int r = 0; r < n && !h->grouped_launch; ++r) {
             const int k = order[r];
             const Plan &p = plans[k];
             GemmArgs g;
@@ -904,7 +1040,7 @@ ozgb_status enqueue_grouped(ozgb_handle h, ozgb_problem *probs, int n, int mode,
         return e == cudaSuccess ? OZGB_OK : cuda_fail(h, e, "grouped slice-pair GEMM launches");
     });
     if (rc) return rc;
-    h->launches += 1 + n;
+    h->launches += 1 + (h->grouped_launch ? static_cast<long long>(launches.size()) : n);
     if (prof) {
         cudaEventRecord(h->ev[3], st);
         h->ev_recorded = true;
@@ -1156,6 +1292,12 @@ ozgb_status ozgb_set_error_criterion(ozgb_handle h, int criterion, double tail) 
     std::lock_guard<std::mutex> lk(h->mu);
     h->err_crit = criterion;
     h->err_tail = tail;
+    return OZGB_OK;
+}
+ozgb_status ozgb_set_grouped_launch(ozgb_handle h, int mode) {
+    if (!h || mode < 0 || mode > 1) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->grouped_launch = mode;
     return OZGB_OK;
 }
 ozgb_status ozgb_set_graph(ozgb_handle h, int enable) {
@@ -1437,6 +1579,89 @@ ozgb_status ozgb_autotune(ozgb_handle h, int M, int N, int K, int bits, int slic
         fill_blocks(best_plan, best);
     }
     return OZGB_OK;
+}
+
+int ozgb_grouped_layout_check(const ozgb_problem *probs, int n, int slices, int bins, int *launches_out,
+                              long long *units_out) {
+    if (!probs || n < 1 || slices < 1) return -1;
+    OzConfig cfg;
+    cfg.b = 7;
+    cfg.s = slices;
+    cfg.J = bins > 0 ? bins : slices;
+    cfg.rounding = OUT_RN;
+    std::vector<Plan> plans(n);
+    for (int i = 0; i < n; ++i) {
+        std::string why;
+        if (probs[i].M < 1 || probs[i].N < 1 || probs[i].K < 1 || probs[i].ldc < probs[i].N) return -2;
+        if (!make_plan(probs[i].M, probs[i].N, probs[i].K, cfg, &plans[i], &why)) return -3;
+    }
+    // stand-in device addresses laid out as enqueue_grouped lays them out
+    const uintptr_t slice_base = uintptr_t(1) << 40, exp_base = uintptr_t(1) << 41;
+    std::vector<const uint8_t *> a_t(n), b_t(n);
+    std::vector<const int32_t *> e_r(n), e_c(n);
+    std::vector<uintptr_t> a_lo(n), b_lo(n), er_lo(n), ec_lo(n);
+    size_t sl = 0, ex = 0;
+    for (int i = 0; i < n; ++i) {
+        a_lo[i] = slice_base + sl;
+        sl += align256(plans[i].a_bytes);
+        b_lo[i] = slice_base + sl;
+        sl += align256(plans[i].b_bytes);
+        er_lo[i] = exp_base + ex;
+        ex += align256(sizeof(int32_t) * probs[i].M);
+        ec_lo[i] = exp_base + ex;
+        ex += align256(sizeof(int32_t) * probs[i].N);
+        a_t[i] = reinterpret_cast<const uint8_t *>(a_lo[i]);
+        b_t[i] = reinterpret_cast<const uint8_t *>(b_lo[i]);
+        e_r[i] = reinterpret_cast<const int32_t *>(er_lo[i]);
+        e_c[i] = reinterpret_cast<const int32_t *>(ec_lo[i]);
+    }
+    int err_word = 0;
+    const std::vector<GroupLaunch> launches =
+        build_group_launches(probs, n, plans, a_t, b_t, e_r, e_c, &err_word, 1000000000ull);
+    long long units = 0;
+    std::vector<std::vector<char>> seen(n);
+    for (int i = 0; i < n; ++i) seen[i].assign(static_cast<size_t>(plans[i].tiles_m) * plans[i].tiles_n, 0);
+    for (const GroupLaunch &L : launches) {
+        const GemmArgs &g = L.g;
+        if (g.total_tiles != static_cast<int>(L.tile_prob.size()) || g.split_parts != 1) return -4;
+        for (int u = 0; u < g.total_tiles; ++u) {
+            const int pi = L.tile_prob[u];
+            if (pi < 0 || pi >= static_cast<int>(L.probs.size())) return -5;
+            const GroupProblem &P = L.probs[pi];
+            TileRef tr;
+            group_tile_ref(L.probs.data(), L.tile_prob.data(), u, g.a_block_bytes, g.b_block_bytes, &tr);
+            // which caller problem this is: by its A slice address
+            int i = -1;
+            for (int q = 0; q < n && i < 0; ++q)
+                if (a_lo[q] == reinterpret_cast<uintptr_t>(P.a_tiles)) i = q;
+            if (i < 0) return -6;
+            const Plan &p = plans[i];
+            if (p.fn != L.plan->fn || p.a_block_bytes != g.a_block_bytes || p.b_block_bytes != g.b_block_bytes ||
+                p.stage_bytes != g.stage_bytes || p.n_kc != tr.n_kc)
+                return -7;
+            if (tr.mt < 0 || tr.mt >= p.tiles_m || tr.nt < 0 || tr.nt >= p.tiles_n) return -8;
+            char &mark = seen[i][static_cast<size_t>(tr.mt) * p.tiles_n + tr.nt];
+            if (mark) return -9;
+            mark = 1;
+            // the producer's bulk copies: chunks [0, n_kc) of the tile's A and B blocks
+            const uintptr_t a0 = reinterpret_cast<uintptr_t>(tr.a_src), b0 = reinterpret_cast<uintptr_t>(tr.b_src);
+            if (a0 < a_lo[i] || a0 + static_cast<size_t>(tr.n_kc) * g.a_block_bytes > a_lo[i] + p.a_bytes) return -10;
+            if (b0 < b_lo[i] || b0 + static_cast<size_t>(tr.n_kc) * g.b_block_bytes > b_lo[i] + p.b_bytes) return -11;
+            if ((a0 | b0) & 15) return -12;
+            // the epilogue: rows below M and columns below N of the tile, C and exponents
+            if (tr.M != probs[i].M || tr.N != probs[i].N || tr.c != probs[i].C || tr.ldc != probs[i].ldc) return -13;
+            if (reinterpret_cast<uintptr_t>(tr.er) != er_lo[i] || reinterpret_cast<uintptr_t>(tr.ec) != ec_lo[i])
+                return -14;
+            if (tr.mt * BM >= tr.M || tr.nt * p.BN >= tr.N) return -15;  // every tile holds output
+            ++units;
+        }
+    }
+    for (int i = 0; i < n; ++i)
+        for (char c : seen[i])
+            if (!c) return -16;
+    if (launches_out) *launches_out = static_cast<int>(launches.size());
+    if (units_out) *units_out = units;
+    return 0;
 }
 
 int ozgb_tuning_entries(void) { return tune_count(); }

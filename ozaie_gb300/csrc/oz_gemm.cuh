@@ -301,7 +301,44 @@ struct TileRef {
     int split;   // index of the split tile (-1: the unit is a whole tile)
 };
 
+// Tile t of a problem whose tiles are rasterised in groups of 8 row tiles that
+// share the same stream of B tiles.
+OZ_HD inline void raster(int t, int tiles_m, int tiles_n, int *mt, int *nt) {
+    const int GM = 8;
+    const int per_group = GM * tiles_n;
+    const int grp = t / per_group;
+    const int first_m = grp * GM;
+    const int gm = (tiles_m - first_m) < GM ? (tiles_m - first_m) : GM;
+    const int rr = t - grp * per_group;
+    *mt = first_m + rr % gm;
+    *nt = rr / gm;
+}
+
+// Work unit u of a grouped launch: problem tile_prob[u], its tile u - tile0.
+// Shared by the kernel and the host-side check of grouped launches.
+OZ_HD inline void group_tile_ref(const GroupProblem *probs, const int *tile_prob, int u, uint32_t a_block_bytes,
+                                 uint32_t b_block_bytes, TileRef *r) {
+    const GroupProblem &P = probs[tile_prob[u]];
+    r->split = -1;
+    r->c0 = 0;
+    r->c1 = P.n_kc;
+    r->er = P.er;
+    r->ec = P.ec;
+    r->c = P.c;
+    r->ldc = P.ldc;
+    r->M = P.M;
+    r->N = P.N;
+    r->n_kc = P.n_kc;
+    raster(u - P.tile0, P.tiles_m, P.tiles_n, &r->mt, &r->nt);
+    r->a_src = P.a_tiles + static_cast<size_t>(r->mt) * P.n_kc * a_block_bytes;
+    r->b_src = P.b_tiles + static_cast<size_t>(r->nt) * P.n_kc * b_block_bytes;
+}
+
 __device__ __forceinline__ void tile_ref(const GemmArgs &g, int u, TileRef *r) {
+    if (g.probs) {
+        group_tile_ref(g.probs, g.tile_prob, u, g.a_block_bytes, g.b_block_bytes, r);
+        return;
+    }
     int t = u, kpart = 0;
     r->split = -1;
     if (g.split_parts > 1 && u >= g.split_start) {
@@ -319,14 +356,7 @@ __device__ __forceinline__ void tile_ref(const GemmArgs &g, int u, TileRef *r) {
     r->M = g.M;
     r->N = g.N;
     r->n_kc = g.n_kc;
-    const int GM = 8;
-    const int per_group = GM * g.tiles_n;
-    const int grp = t / per_group;
-    const int first_m = grp * GM;
-    const int gm = min(GM, g.tiles_m - first_m);
-    const int rr = t - grp * per_group;
-    r->mt = first_m + rr % gm;
-    r->nt = rr / gm;
+    raster(t, g.tiles_m, g.tiles_n, &r->mt, &r->nt);
     r->a_src = reinterpret_cast<const uint8_t *>(g.a_tiles) + static_cast<size_t>(r->mt) * g.n_kc * g.a_block_bytes;
     r->b_src = reinterpret_cast<const uint8_t *>(g.b_tiles) + static_cast<size_t>(r->nt) * g.n_kc * g.b_block_bytes;
 }

@@ -50,6 +50,20 @@ OZ_HD inline long canon_offset8(int r, int kk, int KC) {
     return (long)(((r >> 3) * (KC >> 4) + (kk >> 4)) * 128 + (r & 7) * 16 + (kk & 15));
 }
 
+// One problem of a grouped slice-pair GEMM launch (GemmArgs::probs): every
+// problem of the launch shares the kernel variant, the stage layout, the bin
+// blocks, the drain schedule and the accumulator groups; these are its own.
+struct GroupProblem {
+    const uint8_t *a_tiles;  // its A slice blocks: [tiles_m][n_kc] blocks of a_block_bytes
+    const uint8_t *b_tiles;  // its B slice blocks: [tiles_n][n_kc] blocks of b_block_bytes
+    const int32_t *er;
+    const int32_t *ec;
+    double *c;
+    long ldc;
+    int M, N, n_kc, tiles_m, tiles_n;
+    int tile0;  // its first work unit in the launch
+};
+
 struct GemmArgs {
     const uint16_t *a_tiles;
     const uint16_t *b_tiles;
@@ -79,6 +93,11 @@ struct GemmArgs {
     int blk_period[kMaxGroups], blk_off[kMaxGroups];
     int total_tiles;  // end of the launch's tile range (tiles_m * tiles_n for the whole product)
     int tile_begin;   // first tile of the launch's range (0 for the whole product)
+    // Grouped launch (null otherwise): work unit u < total_tiles is tile
+    // u - probs[p].tile0 of problem p = tile_prob[u]; the per-problem fields above
+    // (operands, sizes, tiles) are then unused.  No K-split in grouped launches.
+    const GroupProblem *probs;
+    const int *tile_prob;
     // Split of the launch's last partial wave along K: work unit u < split_start is
     // tile u over all of K; unit u >= split_start is part (u - split_start) %
     // split_parts of tile split_start + (u - split_start) / split_parts, over chunks

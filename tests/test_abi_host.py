@@ -283,3 +283,19 @@ def test_precision_knob_elementwise_meets_bound(ozlib, oracle, phi):
         C = oracle.dgemm(A, B, 7, s, s, 0)
         rel = np.abs(C - exact)[kept] / np.abs(exact[kept])
         assert rel.max() <= bound, (bound, s, rel.max())
+
+
+def test_grouped_launch_layout_walk(ozlib):
+    """The grouped GEMM launches for the batched workload (512 problems, M, N, K
+    log-uniform in [32, 2048]) and for ragged small shapes, walked on the host the
+    way the kernel walks them: every tile of every problem once, every bulk copy
+    inside its problem's slice blocks, the epilogue on its problem's C."""
+    import bench
+    sizes = [tuple(int(x) for x in r) for r in bench.batched_workload(512)]
+    for s, J in ((9, 9), (8, 15), (4, 7), (12, 12)):
+        rc, n_launch, units = ozlib.grouped_layout_check(sizes, s, J)
+        assert rc == 0, (s, J, rc)
+        assert 1 <= n_launch <= 32 and units > 512
+    small = [(1, 1, 1), (129, 49, 17), (2048, 32, 2048), (32, 2048, 100), (300, 200, 500), (128, 48, 32)]
+    rc, n_launch, units = ozlib.grouped_layout_check(small, 9, 9)
+    assert rc == 0 and units >= len(small)

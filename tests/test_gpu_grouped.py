@@ -34,8 +34,11 @@ def _problems(oracle, rng, n, bounds):
     return probs, host
 
 
+@pytest.mark.parametrize("launch", [1, 0])
 @pytest.mark.parametrize("graph", [0, 1])
-def test_grouped_matches_single_problem_path(gpu_handle, oracle, ozlib, graph):
+def test_grouped_matches_single_problem_path(gpu_handle, oracle, ozlib, graph, launch):
+    """launch 1: one persistent GEMM launch per plan class over all of its
+    problems' tiles; launch 0: one launch per problem."""
     import torch
     rng = np.random.default_rng(7)
     bounds = [1e-15, 0.0, 1e-11, 1e-8, 1e-13]
@@ -43,6 +46,7 @@ def test_grouped_matches_single_problem_path(gpu_handle, oracle, ozlib, graph):
     gpu_handle.set_slices(8)  # problems without a bound use s = 8
     gpu_handle.set_bins(8)
     gpu_handle.set_graph(graph)
+    gpu_handle.set_grouped_launch(launch)
     stream = torch.cuda.current_stream().cuda_stream
     for _ in range(2):  # a second identical call (graph replay when enabled)
         rc, used = gpu_handle.dgemm_grouped(probs, stream)
@@ -109,3 +113,64 @@ def test_grouped_e4m3_slices_match_single_problem_path(gpu_handle, oracle, ozlib
     for (A, B, dA, dB, dC, bound), p in zip(host, probs):
         ref = oracle.dgemm(A, B, 4, 12, 12, 0)
         assert np.array_equal(dC.cpu().numpy().view(np.uint64), ref.view(np.uint64)), (p["M"], p["N"], p["K"])
+
+
+def _check_against_oracle(oracle, host, probs, s):
+    for (A, B, dA, dB, dC, bound), p in zip(host, probs):
+        ref = oracle.dgemm(A, B, 7, s, s, 0)
+        got = dC.cpu().numpy()
+        assert np.array_equal(got.view(np.uint64), ref.view(np.uint64)), (p["M"], p["N"], p["K"])
+
+
+def test_grouped_graph_not_replayed_after_a_call_without_graphs(gpu_handle, oracle):
+    """Calls without graphs rewrite the tables that a captured graph reads: a
+    graph call, a call without graphs on other problems, then the first problems
+    again with graphs must give the oracle's bits each time (the captured graph
+    is not replayed over the rewritten tables)."""
+    import torch
+    stream = torch.cuda.current_stream().cuda_stream
+    gpu_handle.set_slices(7)
+    gpu_handle.set_bins(7)
+    first, host1 = _problems(oracle, np.random.default_rng(31), 6, [0.0])
+    second, host2 = _problems(oracle, np.random.default_rng(32), 9, [0.0])
+    for graph, probs, host in ((1, first, host1), (0, second, host2), (1, first, host1)):
+        for _, _, _, _, dC, _ in host:
+            dC.fill_(float("nan"))
+        gpu_handle.set_graph(graph)
+        rc, _ = gpu_handle.dgemm_grouped(probs, stream)
+        assert rc == 0, gpu_handle.last_error()
+        assert gpu_handle.sync() == 0, gpu_handle.last_error()
+        torch.cuda.synchronize()
+        _check_against_oracle(oracle, host, probs, 7)
+
+
+def test_grouped_many_problems_one_launch_per_class(gpu_handle, oracle, ozlib):
+    """120 problems of 1 to 300 rows and columns, K up to 600, s = 6: a few
+    grouped launches cover every tile once (host walk of the launches), and every
+    result has the oracle's bits."""
+    import torch
+    rng = np.random.default_rng(41)
+    dev = torch.device("cuda", 0)
+    probs, host, sizes = [], [], []
+    for i in range(120):
+        M, N = (int(x) for x in rng.integers(1, 301, 2))
+        K = int(rng.integers(1, 601))
+        A = oracle.gen_phi((M, K), 500 + i, 1.0)
+        B = oracle.gen_phi((K, N), 700 + i, 1.0)
+        dA, dB = torch.from_numpy(A).to(dev), torch.from_numpy(B).to(dev)
+        dC = torch.full((M, N), float("nan"), dtype=torch.float64, device=dev)
+        probs.append({"M": M, "N": N, "K": K, "A": dA.data_ptr(), "lda": K, "B": dB.data_ptr(), "ldb": N,
+                      "C": dC.data_ptr(), "ldc": N})
+        host.append((A, B, dA, dB, dC, 0.0))
+        sizes.append((M, N, K))
+    rc, n_launch, units = ozlib.grouped_layout_check(sizes, 6, 6)
+    assert rc == 0 and 1 <= n_launch <= 12
+    gpu_handle.set_slices(6)
+    gpu_handle.set_bins(6)
+    before = gpu_handle.launch_count()
+    rc, _ = gpu_handle.dgemm_grouped(probs, torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, gpu_handle.last_error()
+    assert gpu_handle.sync() == 0, gpu_handle.last_error()
+    assert gpu_handle.launch_count() - before == 1 + 1 + n_launch  # statistics, splits, GEMMs
+    torch.cuda.synchronize()
+    _check_against_oracle(oracle, host, probs, 6)
