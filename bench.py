@@ -192,22 +192,38 @@ def batched_run(n_probs, dev, stream, oz, O, torch):
     hg.set_graph(1)
 
     def grouped():
-        rc, used = hg.dgemm_grouped(probs, stream.cuda_stream)
+        rc, used = hg.dgemm_grouped(probs, stream.cuda_stream, with_bins=True)
         if rc:
             raise RuntimeError(hg.last_error())
         return used
 
-    for _ in range(3):
-        used = grouped()
-    torch.cuda.synchronize()
-    reps = 5
+    def time_grouped(reps=5):
+        for _ in range(3):
+            u = grouped()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            grouped()
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) / reps * 1e3
+        if hg.sync():
+            raise RuntimeError(hg.last_error())
+        return ms, u
+
+    untuned_ms, used = time_grouped()
+    # the autotuner over the workload's size classes (ceil log2 of M, N, K), for the
+    # slice schedules the grouped call picked; one representative problem per class
+    classes = {}
+    for (m, n, k), sj in zip(sizes, used):
+        key = (int(np.ceil(np.log2(m))), int(np.ceil(np.log2(n))), int(np.ceil(np.log2(k))), sj)
+        classes.setdefault(key, (int(m), int(n), int(k)))
+    ht = oz.Handle()
     t0 = time.perf_counter()
-    for _ in range(reps):
-        grouped()
-    torch.cuda.synchronize()
-    g_ms = (time.perf_counter() - t0) / reps * 1e3
-    if hg.sync():
-        raise RuntimeError(hg.last_error())
+    for (_, _, _, (s_, j_)), (m, n, k) in classes.items():
+        ht.autotune(m, n, k, 7, s_, j_, max_candidates=12)
+    tune_s = time.perf_counter() - t0
+    ht.close()
+    g_ms, used = time_grouped()
     # accuracy: 64 sampled entries of 8 problems against the exact products
     worst = 0.0
     for i in range(0, n_probs, max(1, n_probs // 8)):
@@ -247,19 +263,23 @@ def batched_run(n_probs, dev, stream, oz, O, torch):
             h.set_bins(J)
         return f
 
-    # the grouped call's slice counts (all problems pick the same one here), run per call
-    s_used = int(np.bincount(np.asarray(used)).argmax())
+    # the grouped call's most frequent slice schedule, run per call
+    sched = {}
+    for sj in used:
+        sched[sj] = sched.get(sj, 0) + 1
+    s_used, j_used = max(sched, key=sched.get)
     p_ms = per_call(fixed(8, 15))                       # plain: the accurate configuration
     a_ms = per_call(lambda h: h.set_error_bound(BOUND))  # per-call precision knob
-    e_ms = per_call(fixed(s_used, s_used))               # per-call, the grouped call's s and pair set
+    e_ms = per_call(fixed(s_used, j_used))               # per-call, the grouped call's s and pair set
     return {"workload": "%d DGEMMs, M, N, K log-uniform in [32, 2048] (seed 7), phi=1, bound 1e-15 each" % n_probs,
             "effective_flop": flops,
+            "autotuned_size_classes": {"classes": len(classes), "tuning_s": tune_s,
+                                       "grouped_untuned_ms": untuned_ms},
             "grouped_adaptive_graph": {"value": flops / (g_ms * 1e-3) / 1e12, "unit": UNIT, "ms": g_ms,
-                                       "slices_hist": {str(k): int(v) for k, v in
-                                                       zip(*np.unique(used, return_counts=True))},
+                                       "schedule_hist": {"s%d_J%d" % k: v for k, v in sorted(sched.items())},
                                        "max_normwise_rel_err_sampled": worst},
             "per_call_same_s_triangular": {"value": flops / (e_ms * 1e-3) / 1e12, "unit": UNIT, "ms": e_ms,
-                                           "slices": s_used, "bins": s_used},
+                                           "slices": s_used, "bins": j_used},
             "per_call_adaptive": {"value": flops / (a_ms * 1e-3) / 1e12, "unit": UNIT, "ms": a_ms},
             "plain_per_call_s8_full": {"value": flops / (p_ms * 1e-3) / 1e12, "unit": UNIT, "ms": p_ms},
             "ratios": {
@@ -437,14 +457,16 @@ def mix_run(n, dev, stream, oz, O, torch):
         te = time_device(lambda: call(he, dC), torch, stream)
         if he.sync():
             raise RuntimeError(he.last_error())
-        se = he.config()["slices"]
+        ce = he.config()
+        se = "s%d_J%d" % (ce["slices"], ce["bins"])
         ee = sampled_errors(dA, dB, dC, 256, 1000 + i, O, torch, mpfr=False)
         call(ha, dC)
         ta = time_device(lambda: call(ha, dC), torch, stream)
         for h in (ha, hp, hr):
             if h.sync():
                 raise RuntimeError(h.last_error())
-        s = ha.config()["slices"]
+        ca_ = ha.config()
+        s = "s%d_J%d" % (ca_["slices"], ca_["bins"])
         ea = torch.linalg.norm(dC - dR).item() / rn
         sa = sampled_errors(dA, dB, dC, 256, 1000 + i, O, torch, mpfr=False)
         tc = time_device(lambda: torch.matmul(dA, dB, out=dC), torch, stream)
@@ -459,8 +481,8 @@ def mix_run(n, dev, stream, oz, O, torch):
         worst["normwise_all_vs_16_slices"] = max(worst["normwise_all_vs_16_slices"], ea / bound)
         worst["elementwise_kept_sampled_vs_exact"] = max(worst["elementwise_kept_sampled_vs_exact"],
                                                          ee["max_rel_kept_vs_exact"] / bound)
-        hist[str(s)] = hist.get(str(s), 0) + 1
-        hist_e[str(se)] = hist_e.get(str(se), 0) + 1
+        hist[s] = hist.get(s, 0) + 1
+        hist_e[se] = hist_e.get(se, 0) + 1
         per.append([m, phi, bound, s, se, round(ta, 3), round(te, 3), round(tp, 3), round(tc, 3), ea,
                     sa["normwise_rel_vs_exact"], sa["max_rel_vs_exact"], ee["max_rel_kept_vs_exact"], ep, ec])
         del dA, dB, dR, dC
@@ -475,15 +497,15 @@ def mix_run(n, dev, stream, oz, O, torch):
                                 "whole_matrix_reference_worst_sampled_normwise_vs_exact": ref_worst},
             "bounds_met": met, "problems": len(probs), "worst_err_over_bound": worst,
             "adaptive": {"value": flops_all / (tot["adaptive"] * 1e-3) / 1e12, "unit": UNIT, "ms": tot["adaptive"],
-                         "criterion": "normwise", "slices_hist": hist},
+                         "criterion": "normwise", "schedule_hist": hist},
             "adaptive_elementwise": {"value": flops_all / (tot["adaptive_elementwise"] * 1e-3) / 1e12, "unit": UNIT,
                                      "ms": tot["adaptive_elementwise"], "criterion": "elementwise, tail 1e-4",
-                                     "slices_hist": hist_e},
+                                     "schedule_hist": hist_e},
             "plain_s8_full": {"value": flops_all / (tot["plain_s8_full"] * 1e-3) / 1e12, "unit": UNIT,
                               "ms": tot["plain_s8_full"]},
             "cublas_dgemm": {"value": flops_all / (tot["cublas_dgemm"] * 1e-3) / 1e12, "unit": UNIT,
                              "ms": tot["cublas_dgemm"]},
-            "per_problem": {"columns": ["n", "phi", "bound", "slices", "slices_elementwise", "adaptive_ms",
+            "per_problem": {"columns": ["n", "phi", "bound", "schedule", "schedule_elementwise", "adaptive_ms",
                                         "elementwise_ms", "plain_ms", "cublas_ms", "adaptive_err_all_vs_16",
                                         "adaptive_err_sampled_normwise", "adaptive_err_sampled_max_rel",
                                         "elementwise_err_sampled_max_rel_kept", "plain_err_all_vs_16",
@@ -636,7 +658,10 @@ def main():
     if not args.no_autotune:
         # the precision knob picks s = 9 for this workload: tune that plan (and its
         # neighbours) before anything is timed
-        tuned = {str(s): h.autotune(M, N, K, 7, s, s, max_candidates=24) for s in (8, 9, 10, 11, 12)}
+        # the slice schedules the knob picks here (normwise: s = 8 with the pair
+        # set p + q <= 8; elementwise: s = 11, p + q <= 11) and their neighbours
+        tuned = {"s%d_J%d" % (s, J): h.autotune(M, N, K, 7, s, J, max_candidates=24)
+                 for s, J in ((8, 9), (9, 9), (9, 10), (11, 12), (12, 12))}
     h.set_error_bound(BOUND)
     if args.profile_only and args.slices:
         h.set_slices(args.slices)

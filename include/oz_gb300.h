@@ -145,6 +145,7 @@ typedef struct {
     double *C; long ldc;
     double error_bound; /* requested normwise relative error; <= 0: use the handle's slices */
     int slices_used;    /* out: slices chosen for this problem */
+    int bins_used;      /* out: its pair set, p + q <= bins_used - 1 */
 } ozgb_problem;
 /* Many independent DGEMMs of any sizes (the spec batched form; the
  * reference runs one ozAIE_DGEMM per call, include/oz_aie.h:311).  One launch
@@ -185,6 +186,13 @@ ozgb_status ozgb_set_error_bound(ozgb_handle h, double bound);
  * Both are a-priori estimates from the stage-(a) statistics, not guarantees. */
 enum { OZGB_CRIT_NORMWISE = 0, OZGB_CRIT_ELEMENTWISE = 1 };
 ozgb_status ozgb_set_error_criterion(ozgb_handle h, int criterion, double tail);
+/* The slice schedule the precision knob searches.  1 (default): every slice
+ * count s in [2, 16] and pair set p + q <= J - 1 with s <= J <= 2s - 1; the
+ * knob takes the schedule with the smallest modelled time (the GEMM's UMMA
+ * count on this device plus the split's traffic) whose estimate meets the bound.
+ * 0: the triangular set J = s only (the reference's pair set,
+ * src/aie_kernels/aie2p/mm_ozaki.cc:255-308), smallest s. */
+ozgb_status ozgb_set_schedule_search(ozgb_handle h, int any_pair_set);
 ozgb_status ozgb_set_graph(ozgb_handle h, int enable);     /* capture grouped calls in CUDA graphs */
 /* Grouped calls' slice-pair GEMMs: 1 (default) = one persistent launch per plan
  * class (the problems whose plans share the kernel variant, stage layout, bin
@@ -258,6 +266,13 @@ int ozgb_plan_query(int M, int N, int K, int bits, int slices, int bins, ozgb_co
  * input. */
 int ozgb_choose_slices(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N,
                        const double *sa_k, const double *sb_k, int K, int bits, double bound, double *estimate);
+/* Host-only slice schedule (no device needed): the (slices, bins) the knob picks
+ * on a device with `sms` SMs for an M x N x K product with these statistics,
+ * criterion and tail (ozgb_set_error_criterion) and search (ozgb_set_schedule_search).
+ * Returns 0, or -1 on bad input. */
+int ozgb_choose_schedule(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N,
+                         const double *sa_k, const double *sb_k, int K, int bits, double bound, int criterion,
+                         double tail, int any_pair_set, int sms, int *slices, int *bins, double *estimate);
 /* The same with a criterion and tail as in ozgb_set_error_criterion. */
 int ozgb_choose_slices_ex(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N,
                           const double *sa_k, const double *sb_k, int K, int bits, double bound, int criterion,

@@ -48,6 +48,7 @@ class OzgbProblem(ctypes.Structure):
         ("C", ctypes.c_void_p), ("ldc", ctypes.c_long),
         ("error_bound", ctypes.c_double),
         ("slices_used", ctypes.c_int),
+        ("bins_used", ctypes.c_int),
     ]
 
 
@@ -82,6 +83,9 @@ SIGNATURES = [
     ("ozgb_set_error_criterion", _i, [_h, _i, _dbl]),
     ("ozgb_set_graph", _i, [_h, _i]),
     ("ozgb_set_grouped_launch", _i, [_h, _i]),
+    ("ozgb_set_schedule_search", _i, [_h, _i]),
+    ("ozgb_choose_schedule", _i, [_p, _p, _i, _p, _p, _i, _p, _p, _i, _i, _dbl, _i, _dbl, _i, _i,
+                                  ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_dbl)]),
     ("ozgb_grouped_layout_check", _i, [ctypes.POINTER(OzgbProblem), _i, _i, _i, ctypes.POINTER(_i),
                                        ctypes.POINTER(ctypes.c_longlong)]),
     ("ozgb_set_timeout_ms", _i, [_h, _dbl]),

@@ -112,12 +112,16 @@ class Handle:
         return self._L.ozgb_dgemm_ex(self._h, int(transa), int(transb), M, N, K, float(alpha), dA, lda, dB, ldb,
                                      float(beta), dC, ldc, ctypes.c_void_p(stream or 0))
 
-    def dgemm_grouped(self, problems, stream=None):
+    def dgemm_grouped(self, problems, stream=None, with_bins=False):
+        """Returns (status, slices used per problem), or with with_bins (status,
+        [(slices, bins)] per problem)."""
         arr = (OzgbProblem * len(problems))()
         for i, p in enumerate(problems):
             arr[i] = OzgbProblem(p["M"], p["N"], p["K"], p["A"], p["lda"], p["B"], p["ldb"], p["C"], p["ldc"],
-                                 float(p.get("error_bound", 0.0)), 0)
+                                 float(p.get("error_bound", 0.0)), 0, 0)
         rc = self._L.ozgb_dgemm_grouped(self._h, arr, len(problems), ctypes.c_void_p(stream or 0))
+        if with_bins:
+            return rc, [(arr[i].slices_used, arr[i].bins_used) for i in range(len(problems))]
         return rc, [arr[i].slices_used for i in range(len(problems))]
 
     def sync(self):
@@ -152,6 +156,10 @@ class Handle:
 
     def set_graph(self, on):
         return self._check(self._L.ozgb_set_graph(self._h, 1 if on else 0))
+
+    def set_schedule_search(self, any_pair_set):
+        """1: the knob searches every pair set (default); 0: the triangular set only."""
+        return self._check(self._L.ozgb_set_schedule_search(self._h, int(any_pair_set)))
 
     def set_grouped_launch(self, mode):
         """1: one persistent GEMM launch per plan class (default); 0: one per problem."""
@@ -252,7 +260,7 @@ def grouped_layout_check(sizes, slices, bins=0):
     arr = (OzgbProblem * len(sizes))()
     base = 1 << 42
     for i, (M, N, K) in enumerate(sizes):
-        arr[i] = OzgbProblem(int(M), int(N), int(K), None, int(K), None, int(N), base, int(N), 0.0, 0)
+        arr[i] = OzgbProblem(int(M), int(N), int(K), None, int(K), None, int(N), base, int(N), 0.0, 0, 0)
         base += ((int(M) * int(N) * 8 + 255) // 256) * 256
     nl = ctypes.c_int()
     nu = ctypes.c_longlong()
@@ -283,6 +291,26 @@ def choose_slices(er, ssr, ec, ssc, K, bits, bound, sa_k=None, sb_k=None, criter
                                      None if ka is None else _ptr(ka), None if kb is None else _ptr(kb), int(K),
                                      int(bits), float(bound), int(criterion), float(tail), ctypes.byref(est))
     return s, est.value
+
+
+def choose_schedule(er, ssr, ec, ssc, K, bits, bound, sa_k=None, sb_k=None, criterion=0, tail=1e-4,
+                    any_pair_set=1, sms=152):
+    """Host-only slice schedule: (slices, bins, estimate) that the knob picks for
+    these stage-(a) statistics (M = len(er), N = len(ec)) on a device with `sms` SMs."""
+    er = np.ascontiguousarray(er, np.int32)
+    ec = np.ascontiguousarray(ec, np.int32)
+    ssr = np.ascontiguousarray(ssr, np.float64)
+    ssc = np.ascontiguousarray(ssc, np.float64)
+    ka = None if sa_k is None else np.ascontiguousarray(sa_k, np.float64)
+    kb = None if sb_k is None else np.ascontiguousarray(sb_k, np.float64)
+    s, J, est = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+    rc = load().ozgb_choose_schedule(_ptr(er), _ptr(ssr), er.size, _ptr(ec), _ptr(ssc), ec.size,
+                                     None if ka is None else _ptr(ka), None if kb is None else _ptr(kb), int(K),
+                                     int(bits), float(bound), int(criterion), float(tail), int(any_pair_set), int(sms),
+                                     ctypes.byref(s), ctypes.byref(J), ctypes.byref(est))
+    if rc:
+        raise ValueError("ozgb_choose_schedule: bad input")
+    return s.value, J.value, est.value
 
 
 def convert_paired_i64_to_double_matrix(C, result, M, N, K, num_splits, bits_per_slice):

@@ -62,6 +62,7 @@ struct ozgb_context {
     int profile = OZGB_PROFILE_GB300;
     int opt_bits = 0, opt_slices = 0, opt_bins = 0, opt_rounding = OZGB_ROUND_DEFAULT, opt_format = 0;
     double err_bound = 0.0;
+    int sched_any = 1;             // precision knob: search every pair set (1) or the triangular one only (0)
     int err_crit = KNOB_NORMWISE;  // precision knob: normwise or elementwise criterion
     double err_tail = 1e-4;        // elementwise: entries within err_tail sigma of zero left out
     int use_graph = 0;
@@ -288,6 +289,8 @@ ozgb_status enqueue_exponents(ozgb_handle h, const Operands &o, bool want_ss, cu
     return OZGB_OK;
 }
 
+int sm_count(int dev);
+
 ozgb_status choose_config(ozgb_handle h, const Operands &o, int mode, cudaStream_t st, OzConfig *cfg) {
     *cfg = resolve_config(h, o.K, mode);
     if (h->err_bound > 0.0 && h->opt_slices <= 0) {
@@ -302,10 +305,11 @@ ozgb_status choose_config(ozgb_handle h, const Operands &o, int mode, cudaStream
         cudaMemcpyAsync(&ks, h->knob.p, sizeof ks, cudaMemcpyDeviceToHost, st);
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return cuda_fail(h, e, "statistics readback");
-        double est = 0;
-        const int s = choose_slices_stats(ks, o.K, cfg->b, h->err_bound, 2, 16, &est, h->err_crit, h->err_tail);
-        cfg->s = s;
-        cfg->J = s;
+        // the cheapest slice schedule (slices and pair set) whose estimate meets the bound
+        const Schedule sc = choose_schedule(ks, o.M, o.N, o.K, *cfg, h->err_bound, 2, 16, h->err_crit, h->err_tail,
+                                            h->sched_any != 0, sm_count(h->device));
+        cfg->s = sc.s;
+        cfg->J = sc.J;
     }
     return OZGB_OK;
 }
@@ -881,29 +885,34 @@ ozgb_status enqueue_grouped(ozgb_handle h, ozgb_problem *probs, int n, int mode,
     if (prof) cudaEventRecord(h->ev[1], st);
 
     // ---- precision knob: slice counts from the read-back statistics
-    std::vector<int> s_pick(n, 0);
+    std::vector<Schedule> s_pick(n);
     if (n_adapt > 0) {
         const cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return cuda_fail(h, e, "grouped statistics readback");
         for (int i = 0; i < n; ++i)
-            if (bound[i] > 0.0)
-                s_pick[i] = choose_slices_stats(h->knob_host[adapt_idx[i]], probs[i].K, 7, bound[i], 2, 16, nullptr,
-                                                h->err_crit, h->err_tail);
+            if (bound[i] > 0.0) {
+                OzConfig base = resolve_config(h, probs[i].K, mode);
+                base.b = 7;
+                s_pick[i] = choose_schedule(h->knob_host[adapt_idx[i]], probs[i].M, probs[i].N, probs[i].K, base,
+                                            bound[i], 2, 16, h->err_crit, h->err_tail, h->sched_any != 0,
+                                            sm_count(h->device));
+            }
     }
 
     // ---- plans
     std::vector<Plan> plans(n);
     for (int i = 0; i < n; ++i) {
         OzConfig cfg = resolve_config(h, probs[i].K, mode);
-        if (s_pick[i] > 0) {
+        if (s_pick[i].s > 0) {
             cfg.b = 7;
-            cfg.s = s_pick[i];
-            cfg.J = s_pick[i];
+            cfg.s = s_pick[i].s;
+            cfg.J = s_pick[i].J;
         }
         std::string why;
         if (!make_plan(probs[i].M, probs[i].N, probs[i].K, cfg, &plans[i], &why))
             return fail(h, OZGB_ERR_UNSUPPORTED, "problem " + std::to_string(i) + ": " + why);
         probs[i].slices_used = plans[i].cfg.s;
+        probs[i].bins_used = plans[i].cfg.J;
     }
     // ---- phase 2: stage (b) for every problem (one launch) and the GEMMs
     std::vector<size_t> a_off(n), b_off(n);
@@ -1292,6 +1301,12 @@ ozgb_status ozgb_set_error_criterion(ozgb_handle h, int criterion, double tail) 
     std::lock_guard<std::mutex> lk(h->mu);
     h->err_crit = criterion;
     h->err_tail = tail;
+    return OZGB_OK;
+}
+ozgb_status ozgb_set_schedule_search(ozgb_handle h, int any_pair_set) {
+    if (!h || any_pair_set < 0 || any_pair_set > 1) return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->sched_any = any_pair_set;
     return OZGB_OK;
 }
 ozgb_status ozgb_set_grouped_launch(ozgb_handle h, int mode) {
@@ -1695,6 +1710,24 @@ int ozgb_choose_slices(const int32_t *er, const double *ssr, int M, const int32_
                        const double *sa_k, const double *sb_k, int K, int bits, double bound, double *estimate) {
     return ozgb_choose_slices_ex(er, ssr, M, ec, ssc, N, sa_k, sb_k, K, bits, bound, OZGB_CRIT_NORMWISE, 1e-4,
                                  estimate);
+}
+
+int ozgb_choose_schedule(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N,
+                         const double *sa_k, const double *sb_k, int K, int bits, double bound, int criterion,
+                         double tail, int any_pair_set, int sms, int *slices, int *bins, double *estimate) {
+    if (!er || !ssr || !ec || !ssc || M < 1 || N < 1 || K < 1 || bits < 1 || bits > 7 || !(bound > 0) || sms < 1)
+        return -1;
+    if ((criterion != OZGB_CRIT_NORMWISE && criterion != OZGB_CRIT_ELEMENTWISE) || !(tail > 0.0) || !(tail <= 1.0))
+        return -1;
+    const KnobStats ks = knob_stats_host(er, ssr, M, ec, ssc, N, sa_k, sb_k, K);
+    OzConfig base;
+    base.b = bits;
+    base.rounding = OUT_RN;
+    const Schedule sc = choose_schedule(ks, M, N, K, base, bound, 2, 16, criterion, tail, any_pair_set != 0, sms);
+    if (slices) *slices = sc.s;
+    if (bins) *bins = sc.J;
+    if (estimate) *estimate = sc.est;
+    return 0;
 }
 
 int ozgb_choose_slices_ex(const int32_t *er, const double *ssr, int M, const int32_t *ec, const double *ssc, int N,

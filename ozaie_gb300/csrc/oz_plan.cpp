@@ -562,19 +562,81 @@ std::vector<PlanHints> plan_candidates(int M, int N, int K, const OzConfig &cfg,
 }
 
 double knob_estimate(const KnobStats &k, int K, int b, int s, int crit, double tail) {
+    return knob_estimate_set(k, K, b, s, s, crit, tail);
+}
+
+double knob_estimate_set(const KnobStats &k, int K, int b, int s, int J, int crit, double tail) {
     const double safety = 1.5;
+    // first dropped pairs p + q = J (none for the full set), relative to the tails' 2^{-bs}
+    const double nd = J < 2 * s - 1 ? static_cast<double>(pairs_in_bin(J, s)) : 0.0;
+    const double wd = nd * std::ldexp(1.0, -b * (J - s));
     if (crit == KNOB_ELEMENTWISE) {
+        // the largest of many entries' errors, about 4 of their standard deviations
+        const double safety_max = 4.0;
         if (!(k.ia > 0.0) || !(k.ib > 0.0) || !(tail > 0.0)) return HUGE_VAL;
         const double Kd = static_cast<double>(K);
-        const double r = Kd * (s - 1.0) * (s - 1.0) * k.ia * k.ib / 16.0 + (k.ia + k.ib) / 3.0;
-        const double v = safety * std::ldexp(std::sqrt(Kd * r), -b * s) / tail + std::ldexp(1.0, -53);
+        const double r = Kd * wd * wd * k.ia * k.ib / 16.0 + (k.ia + k.ib) / 3.0;
+        const double v = safety_max * std::ldexp(std::sqrt(Kd * r), -b * s) / tail + std::ldexp(1.0, -53);
         return std::isfinite(v) ? v : HUGE_VAL;
     }
     if (!(k.t > 0.0)) return HUGE_VAL;
-    const double dropped = 0.25 * (s - 1.0) * std::sqrt(static_cast<double>(K) * k.sa * k.sb);
+    const double dropped = 0.25 * wd * std::sqrt(static_cast<double>(K) * k.sa * k.sb);
     const double tails = std::sqrt(k.sa * k.nb / 3.0) + std::sqrt(k.sb * k.na / 3.0);
     const double v = safety * std::ldexp((dropped + tails) / std::sqrt(k.t), -b * s) + std::ldexp(1.0, -53);
     return std::isfinite(v) ? v : HUGE_VAL;
+}
+
+double plan_time_model(const Plan &p, int M, int N, int K, int sms) {
+    const double units = static_cast<double>(p.tiles_m) * p.tiles_n;
+    const double waves = std::ceil(units / std::max(1, sms));
+    const int k_per_umma = p.f8 ? 32 : 16;
+    const double umma_per_chunk = static_cast<double>(p.mma_per_kstep) * (p.KC / k_per_umma);
+    const double gemm_s = waves * p.n_kc * umma_per_chunk * 155.0 / 2.0e9;
+    const double split_bytes = 8.0 * (static_cast<double>(M) * K + static_cast<double>(K) * N) +
+                               static_cast<double>(p.a_bytes + p.b_bytes);
+    return 1e3 * (gemm_s + split_bytes / 6.5e12);
+}
+
+Schedule choose_schedule(const KnobStats &k, int M, int N, int K, const OzConfig &base, double bound, int s_min,
+                         int s_max, int crit, double tail, bool any_set, int sms) {
+    Schedule best;
+    if (!any_set) {
+        // the triangular set: the fewest slices that meet the bound
+        double est = HUGE_VAL;
+        const int s = choose_slices_stats(k, K, base.b, bound, s_min, s_max, &est, crit, tail);
+        best.s = best.J = s;
+        best.est = est;
+        return best;
+    }
+    int first_ok = 0;
+    for (int s = s_min; s <= s_max; ++s) {
+        if (first_ok && s > first_ok + 3) break;  // a product with 4 more slices is not cheaper
+        const int j_max = any_set ? std::min(2 * s - 1, 32) : s;
+        for (int J = s; J <= std::max(s, j_max); ++J) {
+            const double est = knob_estimate_set(k, K, base.b, s, J, crit, tail);
+            if (!(est <= bound)) continue;
+            if (!first_ok) first_ok = s;
+            OzConfig c = base;
+            c.s = s;
+            c.J = J;
+            Plan p;
+            std::string why;
+            if (!make_plan(M, N, K, c, &p, &why)) break;  // a larger J needs at least as much
+            const double ms = plan_time_model(p, M, N, K, sms);
+            if (!best.s || ms < best.ms * (1.0 - 1e-9)) {
+                best.s = s;
+                best.J = J;
+                best.est = est;
+                best.ms = ms;
+            }
+            break;  // the smallest J meeting the bound for this s
+        }
+    }
+    if (!best.s) {
+        best.s = best.J = s_max;
+        best.est = knob_estimate_set(k, K, base.b, s_max, s_max, crit, tail);
+    }
+    return best;
 }
 
 int choose_slices_stats(const KnobStats &k, int K, int b, double bound, int s_min, int s_max, double *estimate,

@@ -120,12 +120,45 @@ enum KnobCriterion : int { KNOB_NORMWISE = 0, KNOB_ELEMENTWISE = 1 };
 // (16 A_i B_j) + 1 / (3 A_i) + 1 / (3 B_j)) (h_ij = 2^{Er_i+Ec_j-2044}
 // sqrt(A_i B_j / K) exactly); the flattest row and column (ia, ib) bound it over
 // all entries:
-//   est_e(s) = 1.5 2^{-bs} sqrt(K) sqrt(K (s-1)^2 ia ib / 16 + (ia + ib) / 3) / tail + 2^{-53}.
+//   est_e(s) = 4 2^{-bs} sqrt(K) sqrt(K (s-1)^2 ia ib / 16 + (ia + ib) / 3) / tail + 2^{-53}
+// (the factor 4: the largest of many entries' errors is about 4 of their
+// standard deviations).
 // No fixed precision bounds the relative error of an entry that cancels to
 // near zero; the tail leaves out the entries within tail h_ij of zero (about a
 // tail's fraction of them for random signs and phi <= 1; more for heavy tails,
 // whose few large terms make h_ij large against most entries).
 double knob_estimate(const KnobStats &k, int K, int b, int s, int crit = KNOB_NORMWISE, double tail = 1e-4);
+
+// The same for the pair set p + q <= J - 1, s <= J <= 2s - 1 (J = s: the
+// triangular set above).  The first dropped pairs are then those with p + q = J,
+// pairs_in_bin(J, s) of them, each of weight 2^{-bJ}/4 on average, so the first
+// term becomes pairs_in_bin(J, s)/4 2^{-bJ} sqrt(K sa sb) (elementwise: likewise
+// inside the square root), while the truncated tails stay at 2^{-bs}.  With the
+// full set (J = 2s - 1) only the tails remain.
+double knob_estimate_set(const KnobStats &k, int K, int b, int s, int J, int crit = KNOB_NORMWISE,
+                         double tail = 1e-4);
+
+// A slice schedule: slices s and pair set J, with its estimate and modelled time.
+struct Schedule {
+    int s = 0, J = 0;
+    double est = 0.0, ms = 0.0;
+};
+
+// Modelled time (ms) of one M x N x K product with a plan on `sms` SMs: the
+// slice-pair GEMM's UMMA count at 155 SM cycles each (measured on GB300 for
+// every N <= 256 and both carriers) at 2 GHz, over whole waves of tiles, plus the
+// HBM traffic of the split at 6.5 TB/s.
+double plan_time_model(const Plan &p, int M, int N, int K, int sms);
+
+// The slice schedule for a requested bound: among s in [s_min, s_max] and, with
+// any_set, every pair set J in [s, 2s - 1] (else J = s only), the one with the
+// smallest modelled time whose estimate meets the bound (ties: fewer slices,
+// then fewer bins).  For each s only the smallest J that meets the bound is a
+// candidate (a larger J only adds pairs).  With none meeting it: (s_max, s_max).
+// Without any_set: the fewest slices s with J = s that meet the bound
+// (choose_slices_stats).
+Schedule choose_schedule(const KnobStats &k, int M, int N, int K, const OzConfig &base, double bound, int s_min,
+                         int s_max, int crit, double tail, bool any_set, int sms);
 
 // Slice count for a requested relative error: the smallest s in [s_min, s_max]
 // with knob_estimate <= bound (s_max if none).  Writes the estimate for the

@@ -238,7 +238,7 @@ def test_plan_slice_format(ozlib, b, s, J):
 
 def test_precision_knob_elementwise_formula(ozlib, oracle):
     """The elementwise estimate against a direct evaluation of its model:
-    est(s) = 1.5 2^-bs sqrt(K) sqrt(K (s-1)^2 ia ib / 16 + (ia + ib) / 3) / tail + 2^-53,
+    est(s) = 4 2^-bs sqrt(K) sqrt(K (s-1)^2 ia ib / 16 + (ia + ib) / 3) / tail + 2^-53,
     ia = max_i 1 / (|a_i|^2 4^(1022 - Er_i)), ib likewise over the columns of B."""
     K = 300
     A = oracle.gen_phi((64, K), 3, 1.0)
@@ -249,7 +249,7 @@ def test_precision_knob_elementwise_formula(ozlib, oracle):
     for tail in (1e-2, 1e-4):
         def model(t):
             r = K * (t - 1) ** 2 * ia * ib / 16 + (ia + ib) / 3
-            return 1.5 * 2.0 ** (-7 * t) * (K * r) ** 0.5 / tail + 2.0 ** -53
+            return 4.0 * 2.0 ** (-7 * t) * (K * r) ** 0.5 / tail + 2.0 ** -53
 
         for bound in (1e-8, 1e-11, 1e-15):
             s, est = ozlib.choose_slices(er, ssr, ec, ssc, K, 7, bound, ca, rb, criterion=1, tail=tail)
@@ -299,3 +299,76 @@ def test_grouped_launch_layout_walk(ozlib):
     small = [(1, 1, 1), (129, 49, 17), (2048, 32, 2048), (32, 2048, 100), (300, 200, 500), (128, 48, 32)]
     rc, n_launch, units = ozlib.grouped_layout_check(small, 9, 9)
     assert rc == 0 and units >= len(small)
+
+
+def test_precision_knob_pair_set_estimate_formula(ozlib, oracle):
+    """The estimate of the pair set p + q <= J - 1 (s <= J <= 2s - 1): the first
+    dropped pairs are the pairs_in_bin(J, s) pairs p + q = J of weight
+    2^(-bJ)/4; the truncated tails stay at 2^(-bs).  J = s is the triangular
+    formula; J = 2s - 1 (the full set) keeps the tails alone."""
+    K = 200
+    A = oracle.gen_phi((64, K), 5, 1.0)
+    B = oracle.gen_phi((K, 48), 6, 1.0)
+    er, ssr, ec, ssc, ca, rb = _stats(A, B)
+    SA = sum(4.0 ** (int(e) - 1022) for e in er)
+    SB = sum(4.0 ** (int(e) - 1022) for e in ec)
+    T = float(np.sum(ca * rb))
+    nA, nB = float(ssr.sum()), float(ssc.sum())
+
+    def pairs(j, s):
+        return max(0, min(j, s - 1) - max(0, j - (s - 1)) + 1)
+
+    def model(s, J):
+        nd = pairs(J, s) if J < 2 * s - 1 else 0
+        return 1.5 * ((nd / 4) * 2.0 ** (-7 * J) * (K * SA * SB) ** 0.5 +
+                      2.0 ** (-7 * s) * ((SA * nB / 3) ** 0.5 + (SB * nA / 3) ** 0.5)) / T ** 0.5 + 2.0 ** -53
+
+    for bound in (1e-8, 1e-11, 1e-13, 1e-15):
+        s, J, est = ozlib.choose_schedule(er, ssr, ec, ssc, K, 7, bound, ca, rb)
+        assert s <= J <= 2 * s - 1
+        assert est == pytest.approx(model(s, J), rel=1e-9) and est <= bound
+        # the triangular search agrees with the slice-only knob
+        st, Jt, _ = ozlib.choose_schedule(er, ssr, ec, ssc, K, 7, bound, ca, rb, any_pair_set=0)
+        assert Jt == st == ozlib.choose_slices(er, ssr, ec, ssc, K, 7, bound, ca, rb)[0]
+
+
+@pytest.mark.parametrize("phi", [0.5, 1.0, 2.0, 4.0])
+def test_slice_schedule_meets_bound(ozlib, oracle, phi):
+    """The slice schedule (s, J) the knob picks when it searches every pair set
+    meets the requested normwise bound on the exact product, and with the
+    elementwise criterion the elementwise bound on every entry at least
+    tail |a_i| |b_j| / sqrt(K) from zero."""
+    tail = 1e-3
+    for (M, N, K), seed in (((96, 80, 300), 13), ((64, 64, 2048), 23)):
+        A = oracle.gen_phi((M, K), seed, phi)
+        B = oracle.gen_phi((K, N), seed + 1, phi)
+        er, ssr, ec, ssc, ca, rb = _stats(A, B)
+        rows = np.repeat(np.arange(M, dtype=np.int32), N)
+        cols = np.tile(np.arange(N, dtype=np.int32), M)
+        exact = oracle.exact_entries(A, B, rows, cols)[0].reshape(M, N)
+        kept = np.abs(exact) >= tail * np.sqrt(np.outer(ssr, ssc) / K)
+        for bound in (1e-8, 1e-11, 1e-13, 1e-15):
+            s, J, _ = ozlib.choose_schedule(er, ssr, ec, ssc, K, 7, bound, ca, rb)
+            C = oracle.dgemm(A, B, 7, s, J, 0)
+            err = np.linalg.norm(C - exact) / np.linalg.norm(exact)
+            assert err <= bound, (bound, s, J, err)
+            s, J, _ = ozlib.choose_schedule(er, ssr, ec, ssc, K, 7, bound, ca, rb, criterion=1, tail=tail)
+            C = oracle.dgemm(A, B, 7, s, J, 0)
+            rel = np.abs(C - exact)[kept] / np.abs(exact[kept])
+            assert rel.max() <= bound, (bound, s, J, rel.max())
+
+
+def test_slice_schedule_prefers_fewer_umma(ozlib):
+    """At 4096^3 with phi = 1 statistics and a 1e-15 normwise bound, the search
+    takes 8 slices with the pair set p + q <= 8 (13 UMMAs per 16-deep K step of a
+    128 x 48 tile) over the triangular 9 slices (14): same bound, less work."""
+    from oracle import ozoracle as O
+    A = O.gen_phi((4096, 4096), 1, 1.0)
+    B = O.gen_phi((4096, 4096), 2, 1.0)
+    er, ssr, ec, ssc, ca, rb = _stats(A, B)
+    s, J, est = ozlib.choose_schedule(er, ssr, ec, ssc, 4096, 7, 1e-15, ca, rb)
+    st, Jt, _ = ozlib.choose_schedule(er, ssr, ec, ssc, 4096, 7, 1e-15, ca, rb, any_pair_set=0)
+    assert (st, Jt) == (9, 9) and (s, J) == (8, 9) and est <= 1e-15
+    a = ozlib.plan_query(4096, 4096, 4096, 7, s, J)
+    b = ozlib.plan_query(4096, 4096, 4096, 7, st, Jt)
+    assert a["umma_per_kstep"] / a["tile_n"] < b["umma_per_kstep"] / b["tile_n"]

@@ -92,15 +92,20 @@ def test_device_knob_matches_host_knob(gpu_handle, oracle, ozlib, phi):
     A = oracle.gen_phi((M, K), 31, phi)
     B = oracle.gen_phi((K, N), 32, phi)
     f = lambda x: ((x.view(np.uint64) >> np.uint64(52)) & np.uint64(0x7FF)).astype(np.int32)
-    for bound in (1e-9, 1e-13, 1e-15):
-        s_host, _ = ozlib.choose_slices(f(A).max(axis=1), (A * A).sum(axis=1), f(B).max(axis=0), (B * B).sum(axis=0),
-                                        K, 7, bound, (A * A).sum(axis=0), (B * B).sum(axis=1))
-        gpu_handle.set_error_bound(bound)
-        C = _dgemm(gpu_handle, A, B, 1)
-        cfg = gpu_handle.config()
-        assert (cfg["slices"], cfg["bins"]) == (s_host, s_host)
-        ref = oracle.dgemm(A, B, 7, s_host, s_host, 0)
-        assert np.array_equal(C.view(np.uint64), ref.view(np.uint64))
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    for any_set in (1, 0):
+        gpu_handle.set_schedule_search(any_set)
+        for bound in (1e-9, 1e-13, 1e-15):
+            s_host, J_host, _ = ozlib.choose_schedule(f(A).max(axis=1), (A * A).sum(axis=1), f(B).max(axis=0),
+                                                      (B * B).sum(axis=0), K, 7, bound, (A * A).sum(axis=0),
+                                                      (B * B).sum(axis=1), any_pair_set=any_set, sms=sms)
+            gpu_handle.set_error_bound(bound)
+            C = _dgemm(gpu_handle, A, B, 1)
+            cfg = gpu_handle.config()
+            assert (cfg["slices"], cfg["bins"]) == (s_host, J_host)
+            ref = oracle.dgemm(A, B, 7, s_host, J_host, 0)
+            assert np.array_equal(C.view(np.uint64), ref.view(np.uint64))
 
 
 @pytest.mark.parametrize("phi", [1.0, 4.0])
@@ -111,14 +116,16 @@ def test_device_elementwise_knob_matches_host_knob(gpu_handle, oracle, ozlib, ph
     A = oracle.gen_phi((M, K), 33, phi)
     B = oracle.gen_phi((K, N), 34, phi)
     f = lambda x: ((x.view(np.uint64) >> np.uint64(52)) & np.uint64(0x7FF)).astype(np.int32)
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
     gpu_handle.set_error_criterion(ozlib.Criterion.elementwise, 1e-3)
     for bound in (1e-9, 1e-13):
-        s_host, _ = ozlib.choose_slices(f(A).max(axis=1), (A * A).sum(axis=1), f(B).max(axis=0), (B * B).sum(axis=0),
-                                        K, 7, bound, (A * A).sum(axis=0), (B * B).sum(axis=1), criterion=1,
-                                        tail=1e-3)
+        s_host, J_host, _ = ozlib.choose_schedule(f(A).max(axis=1), (A * A).sum(axis=1), f(B).max(axis=0),
+                                                  (B * B).sum(axis=0), K, 7, bound, (A * A).sum(axis=0),
+                                                  (B * B).sum(axis=1), criterion=1, tail=1e-3, sms=sms)
         gpu_handle.set_error_bound(bound)
         C = _dgemm(gpu_handle, A, B, 1)
         cfg = gpu_handle.config()
-        assert (cfg["slices"], cfg["bins"]) == (s_host, s_host)
-        ref = oracle.dgemm(A, B, 7, s_host, s_host, 0)
+        assert (cfg["slices"], cfg["bins"]) == (s_host, J_host)
+        ref = oracle.dgemm(A, B, 7, s_host, J_host, 0)
         assert np.array_equal(C.view(np.uint64), ref.view(np.uint64))

@@ -48,22 +48,22 @@ def test_grouped_matches_single_problem_path(gpu_handle, oracle, ozlib, graph, l
     gpu_handle.set_graph(graph)
     gpu_handle.set_grouped_launch(launch)
     stream = torch.cuda.current_stream().cuda_stream
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
     for _ in range(2):  # a second identical call (graph replay when enabled)
-        rc, used = gpu_handle.dgemm_grouped(probs, stream)
+        rc, used = gpu_handle.dgemm_grouped(probs, stream, with_bins=True)
         assert rc == 0, gpu_handle.last_error()
         assert gpu_handle.sync() == 0, gpu_handle.last_error()
     torch.cuda.synchronize()
-    for (A, B, dA, dB, dC, bound), p, s in zip(host, probs, used):
+    for (A, B, dA, dB, dC, bound), p, (s, J) in zip(host, probs, used):
         M, N, K = p["M"], p["N"], p["K"]
         if bound > 0:
             er, ssr, ec, ssc, ca, rb = _stats(A, B)
-            s_host, _ = ozlib.choose_slices(er, ssr, ec, ssc, K, 7, bound, ca, rb)
-            assert s == s_host
+            assert (s, J) == ozlib.choose_schedule(er, ssr, ec, ssc, K, 7, bound, ca, rb, sms=sms)[:2]
         else:
-            assert s == 8
+            assert (s, J) == (8, 8)
         h = ozlib.Handle()
         h.set_slices(s)
-        h.set_bins(s)
+        h.set_bins(J)
         want = torch.full((M, N), float("nan"), dtype=torch.float64, device=dA.device)
         assert h.dgemm_device(M, N, K, dA.data_ptr(), K, dB.data_ptr(), N, want.data_ptr(), N, stream) == 0
         assert h.sync() == 0
