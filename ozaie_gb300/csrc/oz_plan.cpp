@@ -244,15 +244,17 @@ bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std
 
     // ---- bin blocks: contiguous bin ranges of at most 256 columns; every UMMA of a
     // block spans the whole block (zero B slices pad the out-of-range q).  Measured
-    // on GB300: one M=128 K=16 UMMA costs max(~114, N/2) cycles, so the partition
-    // minimising sum(#A slices x cost(N)) is chosen by dynamic programming.
+    // on GB300 with back-to-back UMMAs: every cta_group::1 UMMA costs about 155 SM
+    // cycles whatever its N (16 to 240), M (64 or 128) or kind (f16 or f8f6f4), and
+    // 160 at N = 256, so the partition minimising sum(#A slices x cost(N)), in effect
+    // the UMMA count, is chosen by dynamic programming.
     const int max_groups = kMaxGroups;
     const int maxb = 256 / p.BN;
     auto p0_of = [s](int lo) { return std::max(0, lo - (s - 1)); };
     auto p1_of = [s](int hi) { return std::min(hi, s - 1); };
     auto blk_cost = [&](int lo, int hi) {
         const int nops = p1_of(hi) - p0_of(lo) + 1;
-        return nops * std::max(114.0, (hi - lo + 1) * p.BN / 2.0);
+        return nops * ((hi - lo + 1) * p.BN > 240 ? 160.0 : 155.0);
     };
     const int nbins = B1 - B0 + 1;
     const double INF = 1e300;
