@@ -154,6 +154,56 @@ __device__ __forceinline__ uint32_t slices_e4m3x4(const uint32_t (*w)[5], const 
     return static_cast<uint32_t>(lo) | (static_cast<uint32_t>(hi) << 16);
 }
 
+// One-window split (s b within the first window, see split_two_windows): the
+// slices are then the top s b bits of V = (mantissa << 11) >> bias (0 for
+// bias >= 64), the same bits as split_value's 128-bit window, whose low 64 bits
+// hold no slice.  V is kept as two words plus the element's sign in the two
+// forms the bf16 conversion below uses.
+struct FastElem {
+    uint32_t hi, lo;  // V
+    uint32_t sgnc;    // 0x4B000000 with the sign bit of x
+    float cadd;       // -2^23 for x >= 0, +2^23 for x < 0
+};
+__device__ __forceinline__ FastElem fast_elem(double x, int E) {
+    const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(x));
+    const uint32_t e = static_cast<uint32_t>((u >> 52) & 0x7FF);
+    const unsigned long long mant = (u & ((1ull << 52) - 1)) | (e ? (1ull << 52) : 0ull);
+    const uint32_t bias = static_cast<uint32_t>(E) - e;
+    const unsigned long long v = bias < 64u ? (mant << 11) >> bias : 0ull;
+    const uint32_t neg = static_cast<uint32_t>(u >> 63);
+    FastElem r;
+    r.hi = static_cast<uint32_t>(v >> 32);
+    r.lo = static_cast<uint32_t>(v);
+    r.sgnc = 0x4B000000u | (neg << 31);
+    r.cadd = neg ? 8388608.0f : -8388608.0f;
+    return r;
+}
+// Slice p (B bits at bit B*p from the top of V) as a signed float: the FP32
+// bits of +-(2^23 + v) plus -+2^23 give +-v exactly (and +0 for v = 0): one
+// shift, one three-input logic operation and one add.
+template <int B>
+__device__ __forceinline__ float fast_slice(const FastElem &x, int p) {
+    const int sh = 64 - B * (p + 1);  // V >> sh puts the slice in the low bits
+    const uint32_t f = sh >= 32 ? (x.hi >> (sh - 32)) : __funnelshift_r(x.lo, x.hi, sh);
+    return __uint_as_float((f & ((1u << B) - 1u)) | x.sgnc) + x.cadd;
+}
+// Two floats holding integers of magnitude < 256 as bf16 (exact): lo in bits 0..15.
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+    uint32_t d;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+    return d;
+}
+// 16 bytes of slice p: 8 consecutive K values of one row, as bf16.
+template <int B>
+__device__ __forceinline__ uint4 fast_slice8(const FastElem (&x)[8], int p) {
+    uint4 v;
+    v.x = pack_bf16x2(fast_slice<B>(x[0], p), fast_slice<B>(x[1], p));
+    v.y = pack_bf16x2(fast_slice<B>(x[2], p), fast_slice<B>(x[3], p));
+    v.z = pack_bf16x2(fast_slice<B>(x[4], p), fast_slice<B>(x[5], p));
+    v.w = pack_bf16x2(fast_slice<B>(x[6], p), fast_slice<B>(x[7], p));
+    return v;
+}
+
 __host__ __device__ inline bool split_two_windows(int b, int s) {
     const int avoid = 1 + (b == 3 ? 3 : 0);
     const int nv0 = 64 - avoid - ((64 - avoid) % b);
@@ -175,8 +225,38 @@ __device__ __forceinline__ void split_a_body(const double *__restrict__ A, long 
     if (m >= Mp || k0 >= Kp) return;
     const bool two = split_two_windows(B, s);
     const int E = m < M ? er[m] : 0;
-    uint32_t w[8][5], sg[8];
     const double *row = A + static_cast<size_t>(m) * lda;
+    if (!F8 && !two) {
+        // one window: 128-bit loads where the row's 8 values are in range and
+        // aligned, the shift-and-add slice conversion
+        double xv[8];
+        const double *src = row + k0;
+        if (!trans && m < M && k0 + 8 <= K && (reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const double2 d = __ldg(reinterpret_cast<const double2 *>(src) + i);
+                xv[2 * i] = d.x;
+                xv[2 * i + 1] = d.y;
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int k = k0 + i;
+                xv[i] = (m < M && k < K) ? __ldg(trans ? A + static_cast<size_t>(k) * lda + m : row + k) : 0.0;
+            }
+        }
+        FastElem fe[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) fe[i] = fast_elem(xv[i], E);
+        const int mt = m >> 7, r = m & 127, c = k0 / KC, kk = k0 % KC;
+        const size_t slice_elems = static_cast<size_t>(BM) * KC;
+        uint16_t *dst = tiles + (static_cast<size_t>(mt) * n_kc + c) * s * slice_elems + canon_offset(r, kk, KC);
+#pragma unroll
+        for (int p = 0; p < 64 / B; ++p)
+            if (p < s) *reinterpret_cast<uint4 *>(dst + p * slice_elems) = fast_slice8<B>(fe, p);
+        return;
+    }
+    uint32_t w[8][5], sg[8];
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         const int k = k0 + i;
@@ -232,6 +312,25 @@ __device__ __forceinline__ void split_b_body(const double *__restrict__ Bm, long
     if (n >= Np || k0 >= Kp) return;
     const bool two = split_two_windows(B, s);
     const int E = n < N ? ec[n] : 0;
+    if (!F8 && !two) {
+        // one window: the shift-and-add slice conversion
+        FastElem fe[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int k = k0 + i;
+            const double x = (n < N && k < K) ? __ldg(trans ? Bm + static_cast<size_t>(n) * ldb + k
+                                                            : Bm + static_cast<size_t>(k) * ldb + n)
+                                              : 0.0;
+            fe[i] = fast_elem(x, E);
+        }
+        const int nt = n / BN, r = n % BN, c = k0 / KC, kk = k0 % KC;
+        const size_t slice_elems = static_cast<size_t>(BN) * KC;
+        uint16_t *dst = tiles + (static_cast<size_t>(nt) * n_kc + c) * s * slice_elems + canon_offset(r, kk, KC);
+#pragma unroll
+        for (int q = 0; q < 64 / B; ++q)
+            if (q < s) *reinterpret_cast<uint4 *>(dst + q * slice_elems) = fast_slice8<B>(fe, q);
+        return;
+    }
     uint32_t w[8][5], sg[8];
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
