@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 
 #include "oz_internal.h"
@@ -796,16 +797,20 @@ __device__ __forceinline__ void run_stage_job(const StageJob &j, int local) {
     }
 }
 
+// Persistent: block b runs work blocks b, b + gridDim.x, ... of the job list; the
+// job of a work block is found by a forward scan from the previous one (work
+// blocks only increase), so no block pays a search over all jobs, and a grouped
+// call of many small problems does not launch one block per 2048 elements.
 __global__ void __launch_bounds__(kStageThreads) k_stage_jobs(const StageJob *__restrict__ jobs,
                                                               const int *__restrict__ block0, int n_jobs) {
-    int lo = 0, hi = n_jobs - 1;
-    const int bid = blockIdx.x;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (__ldg(block0 + mid) <= bid) lo = mid;
-        else hi = mid - 1;
+    const int total = __ldg(block0 + n_jobs);
+    int j = 0;
+    for (int bid = blockIdx.x; bid < total; bid += gridDim.x) {
+        while (j + 1 < n_jobs && __ldg(block0 + j + 1) <= bid) ++j;
+        run_stage_job<false>(jobs[j], bid - __ldg(block0 + j));
+        // the statistics job's shared memory is written again by the next work block
+        __syncthreads();
     }
-    run_stage_job<false>(jobs[lo], bid - __ldg(block0 + lo));
 }
 
 // Two jobs of one problem (A and B) in one launch: blocks [0, n0) run j0.
@@ -882,8 +887,25 @@ void launch_stage_pair(StageJob j0, StageJob j1, void *stream) {
 }
 
 void launch_stage_jobs(const StageJob *jobs, const int *block0, int n_jobs, int total_blocks, void *stream) {
-    if (total_blocks > 0)
-        k_stage_jobs<<<total_blocks, kStageThreads, 0, static_cast<cudaStream_t>(stream)>>>(jobs, block0, n_jobs);
+    if (total_blocks <= 0) return;
+    // resident blocks of k_stage_jobs on the current device, found once per device
+    static std::atomic<int> resident[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int grid = 0;
+    if (dev >= 0 && dev < 64) grid = resident[dev].load(std::memory_order_relaxed);
+    if (grid <= 0) {
+        int sms = 0, per_sm = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 148;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_jobs, kStageThreads, 0) != cudaSuccess ||
+            per_sm <= 0)
+            per_sm = 2;
+        cudaGetLastError();
+        grid = sms * per_sm;
+        if (dev >= 0 && dev < 64) resident[dev].store(grid, std::memory_order_relaxed);
+    }
+    k_stage_jobs<<<std::min(grid, total_blocks), kStageThreads, 0, static_cast<cudaStream_t>(stream)>>>(jobs, block0,
+                                                                                                      n_jobs);
 }
 
 void launch_knob_grouped(const KnobJob *jobs, int n, void *stream) {
