@@ -59,7 +59,7 @@ def load_peaks():
 
 def profile_traffic():
     """Per-launch DRAM bytes of the slice-pair GEMM from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "oz_gemm_kernel_4096_s9.md")
+    p = os.path.join(ROOT, "profiles", "oz_gemm_kernel_4096_s8_j9.md")
     if not os.path.exists(p):
         return None
     with open(p) as f:
