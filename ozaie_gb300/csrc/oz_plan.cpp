@@ -244,17 +244,18 @@ bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std
 
     // ---- bin blocks: contiguous bin ranges of at most 256 columns; every UMMA of a
     // block spans the whole block (zero B slices pad the out-of-range q).  Measured
-    // on GB300 with back-to-back UMMAs: every cta_group::1 UMMA costs about 155 SM
-    // cycles whatever its N (16 to 240), M (64 or 128) or kind (f16 or f8f6f4), and
-    // 160 at N = 256, so the partition minimising sum(#A slices x cost(N)), in effect
-    // the UMMA count, is chosen by dynamic programming.
+    // on GB300 with back-to-back UMMAs (tests/perf/umma_cost.cu): a cta_group::1
+    // UMMA costs a floor of about 140-155 SM cycles whatever its N up to about 200,
+    // its M (64 or 128) or its kind (f16 or f8f6f4), and about 0.66 cycles per
+    // column above that (160-170 at N = 256), so the partition minimising
+    // sum(#A slices x cost(N)), nearly the UMMA count, is chosen by dynamic programming.
     const int max_groups = kMaxGroups;
     const int maxb = 256 / p.BN;
     auto p0_of = [s](int lo) { return std::max(0, lo - (s - 1)); };
     auto p1_of = [s](int hi) { return std::min(hi, s - 1); };
     auto blk_cost = [&](int lo, int hi) {
         const int nops = p1_of(hi) - p0_of(lo) + 1;
-        return nops * ((hi - lo + 1) * p.BN > 240 ? 160.0 : 155.0);
+        return nops * std::max(150.0, 0.66 * (hi - lo + 1) * p.BN);
     };
     const int nbins = B1 - B0 + 1;
     const double INF = 1e300;
