@@ -223,6 +223,11 @@ def batched_run(n_probs, dev, stream, oz, O, torch):
         ht.autotune(m, n, k, 7, s_, j_, max_candidates=12)
     tune_s = time.perf_counter() - t0
     ht.close()
+    tuned_ms, _ = time_grouped()
+    # the per-class winners, each timed alone, spread the problems over more plan
+    # classes (grouped launches); the grouped call is timed again with the
+    # planner's own plans (the tuning table cleared), which measured faster
+    oz.load().ozgb_tuning_clear()
     g_ms, used = time_grouped()
     # accuracy: 64 sampled entries of 8 problems against the exact products
     worst = 0.0
@@ -273,8 +278,10 @@ def batched_run(n_probs, dev, stream, oz, O, torch):
     e_ms = per_call(fixed(s_used, j_used))               # per-call, the grouped call's s and pair set
     return {"workload": "%d DGEMMs, M, N, K log-uniform in [32, 2048] (seed 7), phi=1, bound 1e-15 each" % n_probs,
             "effective_flop": flops,
-            "autotuned_size_classes": {"classes": len(classes), "tuning_s": tune_s,
-                                       "grouped_untuned_ms": untuned_ms},
+            "autotuned_size_classes": {"classes": len(classes), "tuning_s": tune_s, "grouped_tuned_ms": tuned_ms,
+                                       "grouped_untuned_first_ms": untuned_ms,
+                                       "note": "per-class winners timed alone; the grouped call below uses the "
+                                               "planner's plans (the tuning table cleared)"},
             "grouped_adaptive_graph": {"value": flops / (g_ms * 1e-3) / 1e12, "unit": UNIT, "ms": g_ms,
                                        "schedule_hist": {"s%d_J%d" % k: v for k, v in sorted(sched.items())},
                                        "max_normwise_rel_err_sampled": worst},
