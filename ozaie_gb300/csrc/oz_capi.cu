@@ -684,14 +684,35 @@ struct GroupLaunch {
     double cost = 0.0;  // tiles x chunks x pairs
 };
 
-std::vector<long long> launch_key(const GemmArgs &g, const Plan &p) {
-    std::vector<long long> k = {reinterpret_cast<long long>(p.fn), static_cast<long long>(p.smem), g.KC, g.s, g.J,
+// The launch-level fields of a plan's GemmArgs as a fixed array (no allocation):
+// problems with equal arrays share a grouped launch.
+constexpr int kLaunchFields = 17 + kMaxAcc + 6 * kMaxGroups;
+struct LaunchFields {
+    long long v[kLaunchFields];
+    int n = 0;
+    unsigned long long hash = 0;
+};
+LaunchFields launch_fields(const GemmArgs &g, const Plan &p) {
+    LaunchFields f;
+    const long long head[17] = {reinterpret_cast<long long>(p.fn), static_cast<long long>(p.smem), g.KC, g.s, g.J,
                                 g.b, g.out_mode, g.stages, g.stage_bytes, g.a_block_bytes, g.b_block_bytes,
                                 g.b_pad_lo_bytes, g.b_region_bytes, g.tmem_cols, g.n_acc, g.n_iss, g.G};
-    for (int a = 0; a < kMaxAcc; ++a) k.push_back(g.acc_t0[a]);
+    for (long long x : head) f.v[f.n++] = x;
+    for (int a = 0; a < kMaxAcc; ++a) f.v[f.n++] = g.acc_t0[a];
     for (int i = 0; i < g.G; ++i)
-        k.insert(k.end(), {g.blk_lo[i], g.blk_nb[i], g.blk_p0[i], g.blk_p1[i], g.blk_period[i], g.blk_off[i]});
-    return k;
+        for (long long x : {g.blk_lo[i], g.blk_nb[i], g.blk_p0[i], g.blk_p1[i], g.blk_period[i], g.blk_off[i]})
+            f.v[f.n++] = x;
+    unsigned long long h = 1469598103934665603ull;  // FNV-1a over the words
+    for (int i = 0; i < f.n; ++i) h = (h ^ static_cast<unsigned long long>(f.v[i])) * 1099511628211ull;
+    f.hash = h;
+    return f;
+}
+bool same_launch(const LaunchFields &x, const LaunchFields &y) {
+    return x.hash == y.hash && x.n == y.n && std::equal(x.v, x.v + x.n, y.v);
+}
+std::vector<long long> launch_key(const GemmArgs &g, const Plan &p) {
+    const LaunchFields f = launch_fields(g, p);
+    return std::vector<long long>(f.v, f.v + f.n);
 }
 
 // The grouped launches of n problems with the given plans and device addresses
@@ -709,20 +730,21 @@ std::vector<GroupLaunch> build_group_launches(const ozgb_problem *probs, int n, 
     };
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost(x) > cost(y); });
     std::vector<GroupLaunch> out;
-    std::map<std::vector<long long>, size_t> index;
+    std::vector<LaunchFields> keys;  // of out's launches (few: a linear scan of hashes)
     for (int i : order) {
         const Plan &p = plans[i];
         GemmArgs g;
         gemm_args_from_plan(&g, p, p.cfg.rounding, err, timeout_ns);
-        const std::vector<long long> key = launch_key(g, p);
-        auto it = index.find(key);
-        if (it == index.end()) {
-            it = index.emplace(key, out.size()).first;
+        const LaunchFields key = launch_fields(g, p);
+        size_t li = 0;
+        while (li < keys.size() && !same_launch(keys[li], key)) ++li;
+        if (li == keys.size()) {
+            keys.push_back(key);
             out.emplace_back();
             out.back().g = g;
             out.back().plan = &p;
         }
-        GroupLaunch &L = out[it->second];
+        GroupLaunch &L = out[li];
         GroupProblem gp{};
         gp.a_tiles = a_tiles[i];
         gp.b_tiles = b_tiles[i];
@@ -1634,6 +1656,8 @@ int ozgb_grouped_layout_check(const ozgb_problem *probs, int n, int slices, int 
     const std::vector<GroupLaunch> launches =
         build_group_launches(probs, n, plans, a_t, b_t, e_r, e_c, &err_word, 1000000000ull);
     long long units = 0;
+    std::map<uintptr_t, int> by_a;
+    for (int i = 0; i < n; ++i) by_a[a_lo[i]] = i;
     std::vector<std::vector<char>> seen(n);
     for (int i = 0; i < n; ++i) seen[i].assign(static_cast<size_t>(plans[i].tiles_m) * plans[i].tiles_n, 0);
     for (const GroupLaunch &L : launches) {
@@ -1646,10 +1670,9 @@ int ozgb_grouped_layout_check(const ozgb_problem *probs, int n, int slices, int 
             TileRef tr;
             group_tile_ref(L.probs.data(), L.tile_prob.data(), u, g.a_block_bytes, g.b_block_bytes, &tr);
             // which caller problem this is: by its A slice address
-            int i = -1;
-            for (int q = 0; q < n && i < 0; ++q)
-                if (a_lo[q] == reinterpret_cast<uintptr_t>(P.a_tiles)) i = q;
-            if (i < 0) return -6;
+            const auto found = by_a.find(reinterpret_cast<uintptr_t>(P.a_tiles));
+            if (found == by_a.end()) return -6;
+            const int i = found->second;
             const Plan &p = plans[i];
             if (p.fn != L.plan->fn || p.a_block_bytes != g.a_block_bytes || p.b_block_bytes != g.b_block_bytes ||
                 p.stage_bytes != g.stage_bytes || p.n_kc != tr.n_kc)

@@ -7,6 +7,7 @@
 #include <map>
 #include <mutex>
 #include <tuple>
+#include <unordered_map>
 #include <vector>
 
 namespace ozgb {
@@ -103,8 +104,18 @@ namespace {
 // Plans without hints are pure functions of the shape, the configuration and the
 // tuning table: cached, so that grouped calls with many problems plan in O(1) each.
 using PlanKey = std::tuple<int, int, int, int, int, int, int, int, int, int, long>;
+struct PlanKeyHash {
+    size_t operator()(const PlanKey &k) const {
+        const long long v[11] = {std::get<0>(k), std::get<1>(k), std::get<2>(k), std::get<3>(k),
+                                 std::get<4>(k), std::get<5>(k), std::get<6>(k), std::get<7>(k),
+                                 std::get<8>(k), std::get<9>(k), std::get<10>(k)};
+        unsigned long long h = 1469598103934665603ull;  // FNV-1a
+        for (long long x : v) h = (h ^ static_cast<unsigned long long>(x)) * 1099511628211ull;
+        return static_cast<size_t>(h);
+    }
+};
 std::mutex g_plan_mu;
-std::map<PlanKey, Plan> g_plans;
+std::unordered_map<PlanKey, Plan, PlanKeyHash> g_plans;
 }  // namespace
 
 bool make_plan(int M, int N, int K, const OzConfig &cfg, Plan *out, std::string *err, int bin_lo, int bin_hi,
