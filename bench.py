@@ -622,6 +622,23 @@ def profile_grouped(n_probs):
         out["launch_per_class" if launch else "launch_per_problem"] = {
             "stage_ms": h.stage_times(), "launches_per_call": (h.launch_count() - n0) / 6}
         h.close()
+    # wall time per call (five calls back to back) of the default form, with and without graphs
+    for graph in (0, 1):
+        h = oz.Handle()
+        h.set_graph(graph)
+        for _ in range(3):
+            h.dgemm_grouped(probs, stream)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(5):
+            rc, _ = h.dgemm_grouped(probs, stream)
+            if rc:
+                raise RuntimeError(h.last_error())
+        torch.cuda.synchronize()
+        out["wall_ms_graph%d" % graph] = (time.perf_counter() - t0) / 5 * 1e3
+        if h.sync():
+            raise RuntimeError(h.last_error())
+        h.close()
     print(json.dumps({"profile_grouped": True, "problems": n_probs, **out}))
     return 0
 

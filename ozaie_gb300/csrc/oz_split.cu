@@ -537,27 +537,45 @@ __device__ __forceinline__ void stats2d_body(const double *__restrict__ X, long 
     for (int i = wid; i < kStatsRows; i += NW) {
         const int r = r0 + i;
         load_row(r, x);
+        int ex[CPL];
+        uint32_t mb[CPL];  // FP32 mantissa bits of each element; 0 for zeros, subnormals, non-finite
         int Er = 0;
-        float sr = 0.0f;
 #pragma unroll
         for (int k = 0; k < CPL; ++k) {
             const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(x[k]));
-            const int e = static_cast<int>((bits >> 52) & 0x7FF);
-            float m2 = 0.0f;
-            if (e != 0 && e != 0x7FF) {
-                const float m = __uint_as_float(0x3F800000u | static_cast<uint32_t>((bits >> 29) & 0x7FFFFF));
-                m2 = m * m;
+            ex[k] = static_cast<int>((bits >> 52) & 0x7FF);
+            mb[k] = (ex[k] != 0 && ex[k] != 0x7FF) ? (0x800000u | static_cast<uint32_t>((bits >> 29) & 0x7FFFFF)) : 0u;
+            Er = max(Er, ex[k]);
+        }
+        // columns: running exponent per column, rescaled only when a larger one
+        // appears (rare after the first rows); x scaled by 2^(-Ec) squared by one FMA
+#pragma unroll
+        for (int k = 0; k < CPL; ++k) {
+            if (ex[k] > Ec[k]) {
+                sc[k] *= pow4f(Ec[k] - ex[k]);
+                Ec[k] = ex[k];
             }
-            sq_add_em(Ec[k], sc[k], e, m2);
-            sq_add_em(Er, sr, e, m2);
+            const int d = ex[k] - Ec[k];
+            const float xs = (mb[k] && d >= -63) ? __uint_as_float((static_cast<uint32_t>(d + 127) << 23) |
+                                                                   (mb[k] & 0x7FFFFFu))
+                                                 : 0.0f;
+            sc[k] = fmaf(xs, xs, sc[k]);
         }
         if (rows_wanted) {
+            // rows: one exponent for the whole row (the warp's maximum), then plain sums
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const int e2 = __shfl_xor_sync(0xffffffffu, Er, o);
-                const float s2 = __shfl_xor_sync(0xffffffffu, sr, o);
-                sq_merge(Er, sr, e2, s2);
+            for (int o = 16; o > 0; o >>= 1) Er = max(Er, __shfl_xor_sync(0xffffffffu, Er, o));
+            float sr = 0.0f;
+#pragma unroll
+            for (int k = 0; k < CPL; ++k) {
+                const int d = ex[k] - Er;
+                const float xs = (mb[k] && d >= -63) ? __uint_as_float((static_cast<uint32_t>(d + 127) << 23) |
+                                                                       (mb[k] & 0x7FFFFFu))
+                                                     : 0.0f;
+                sr = fmaf(xs, xs, sr);
             }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) sr += __shfl_xor_sync(0xffffffffu, sr, o);
             if (lane == 0 && r < rows) {
                 if (row_part) row_part[static_cast<size_t>(r) * nbx + bx] = sq_pack(Er, sr);
                 if (row_e) atomicMax(row_e + r, Er);
