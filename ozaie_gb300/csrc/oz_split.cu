@@ -533,10 +533,14 @@ __device__ __forceinline__ void stats2d_body(const double *__restrict__ X, long 
         for (int k = 0; k < CPL; ++k)
             x[k] = (r < rows && c0 + 32 * k < cols) ? __ldg(X + static_cast<size_t>(r) * ld + c0 + 32 * k) : 0.0;
     };
-    double x[CPL];
+    // the next row's loads are issued before this row is reduced
+    double x[CPL], xn[CPL];
+    if (wid < kStatsRows) load_row(r0 + wid, xn);
     for (int i = wid; i < kStatsRows; i += NW) {
         const int r = r0 + i;
-        load_row(r, x);
+#pragma unroll
+        for (int k = 0; k < CPL; ++k) x[k] = xn[k];
+        if (i + NW < kStatsRows) load_row(r + NW, xn);
         int ex[CPL];
         uint32_t mb[CPL];  // FP32 mantissa bits of each element; 0 for zeros, subnormals, non-finite
         int Er = 0;
