@@ -79,8 +79,9 @@ typedef struct {
     int umma_per_kstep; /* UMMAs per 16-deep K step */
     int block_lo[8]; /* first bin of each block */
     int block_nb[8]; /* bins in each block */
-    int issuers;     /* threads issuing the UMMAs (bin blocks split between them) */
+    int issuers;     /* warps issuing the UMMAs (1 to 3; the UMMA runs of a K step dealt round-robin) */
     int slice_format;/* 0: bf16 slices (kind::f16); 1: e4m3 slices (kind::f8f6f4, b <= 4) */
+    int dbl_blocks;  /* bit g: block g has two accumulator ranges, its UMMAs go on while one drains */
 } ozgb_config;
 
 /* ---------------------------------------------------------------- handles */
@@ -169,6 +170,14 @@ ozgb_status ozgb_set_rounding(ozgb_handle h, int rounding);
 /* Slice format: 0 = e4m3 where it is exact (b <= 4) and a kernel fits, else bf16
  * (default); 1 = bf16 always. */
 ozgb_status ozgb_set_slice_format(ozgb_handle h, int format);
+/* Fixes choices of the slice-pair GEMM plan for this handle's single calls (0 =
+ * the planner's choice): tile width tile_n (16..128), K chunk, pipeline stages,
+ * issuing warps (1 to 3), double-buffered blocks (dbl: -1 the planner's
+ * choice, 0 none, 1 every block that fits TMEM), and `blocks` bin-block sizes
+ * block_nb[0..blocks) covering the bins.  All zeros and dbl = -1 clear it.  A
+ * call whose plan cannot honour the hint fails with OZGB_ERR_UNSUPPORTED. */
+ozgb_status ozgb_set_plan_hint(ozgb_handle h, int tile_n, int k_chunk, int stages, int issuers, int dbl, int blocks,
+                               const int *block_nb);
 /* Requested relative error (> 0 enables slice selection from the exponent
  * spread measured by stage (a)); 0 disables it.  The error it bounds is set by
  * ozgb_set_error_criterion (normwise by default). */

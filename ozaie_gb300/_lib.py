@@ -30,6 +30,7 @@ class OzgbConfig(ctypes.Structure):
         ("block_nb", ctypes.c_int * 8),
         ("issuers", ctypes.c_int),
         ("slice_format", ctypes.c_int),
+        ("dbl_blocks", ctypes.c_int),
     ]
 
     def as_dict(self):
@@ -79,6 +80,7 @@ SIGNATURES = [
     ("ozgb_set_bins", _i, [_h, _i]),
     ("ozgb_set_rounding", _i, [_h, _i]),
     ("ozgb_set_slice_format", _i, [_h, _i]),
+    ("ozgb_set_plan_hint", _i, [_h, _i, _i, _i, _i, _i, _i, ctypes.c_void_p]),
     ("ozgb_set_error_bound", _i, [_h, _dbl]),
     ("ozgb_set_error_criterion", _i, [_h, _i, _dbl]),
     ("ozgb_set_graph", _i, [_h, _i]),

@@ -143,6 +143,13 @@ class Handle:
     def set_rounding(self, r):
         return self._check(self._L.ozgb_set_rounding(self._h, int(r)))
 
+    def set_plan_hint(self, tile_n=0, k_chunk=0, stages=0, issuers=0, dbl=-1, block_nb=()):
+        """Fix choices of the slice-pair GEMM plan (0 / -1 / () = the planner's)."""
+        arr = (ctypes.c_int * max(1, len(block_nb)))(*block_nb) if block_nb else None
+        return self._check(self._L.ozgb_set_plan_hint(self._h, int(tile_n), int(k_chunk), int(stages),
+                                                      int(issuers), int(dbl), len(block_nb),
+                                                      ctypes.cast(arr, ctypes.c_void_p) if arr else None))
+
     def set_slice_format(self, fmt):
         """0: e4m3 slices where exact (b <= 4), else bf16; 1: bf16 always."""
         return self._check(self._L.ozgb_set_slice_format(self._h, int(fmt)))

@@ -67,6 +67,8 @@ struct ozgb_context {
     double err_tail = 1e-4;        // elementwise: entries within err_tail sigma of zero left out
     int use_graph = 0;
     unsigned long long timeout_ns = 2000000000ull;
+    bool have_plan_hint = false;  // ozgb_set_plan_hint: fixed GEMM plan choices for single calls
+    PlanHints plan_hint{};
     // last effective plan
     Plan last{};
     bool have_last = false;
@@ -345,7 +347,9 @@ void gemm_args_from_plan(GemmArgs *g, const Plan &p, int out_mode, int *err, uns
         g->blk_p1[i] = p.blk_p1[i];
         g->blk_period[i] = p.blk_period[i];
         g->blk_off[i] = p.blk_off[i];
+        g->blk_col1[i] = p.blk_col1[i];
     }
+    g->dbl_mask = p.dbl_mask;
 }
 
 // Auxiliary streams and their events, created on first use.
@@ -579,7 +583,12 @@ ozgb_status enqueue_dgemm(ozgb_handle h, const Operands &o, int mode, cudaStream
         if (cfg.J != cfg.s) return fail(h, OZGB_ERR_UNSUPPORTED, "paired output needs the triangular pair set");
         pairs_hint.min_W = 4;
     }
-    if (!make_plan(o.M, o.N, o.K, cfg, &p, &why, bin_lo, bin_hi, pairs ? &pairs_hint : nullptr))
+    if (h->have_plan_hint) {
+        const int min_w = pairs_hint.min_W;
+        pairs_hint = h->plan_hint;
+        pairs_hint.min_W = min_w;
+    }
+    if (!make_plan(o.M, o.N, o.K, cfg, &p, &why, bin_lo, bin_hi, pairs || h->have_plan_hint ? &pairs_hint : nullptr))
         return fail(h, OZGB_ERR_UNSUPPORTED, why);
     h->last = p;
     h->have_last = true;
@@ -686,7 +695,7 @@ struct GroupLaunch {
 
 // The launch-level fields of a plan's GemmArgs as a fixed array (no allocation):
 // problems with equal arrays share a grouped launch.
-constexpr int kLaunchFields = 17 + kMaxAcc + 6 * kMaxGroups;
+constexpr int kLaunchFields = 18 + kMaxAcc + 7 * kMaxGroups;
 struct LaunchFields {
     long long v[kLaunchFields];
     int n = 0;
@@ -694,13 +703,14 @@ struct LaunchFields {
 };
 LaunchFields launch_fields(const GemmArgs &g, const Plan &p) {
     LaunchFields f;
-    const long long head[17] = {reinterpret_cast<long long>(p.fn), static_cast<long long>(p.smem), g.KC, g.s, g.J,
+    const long long head[18] = {reinterpret_cast<long long>(p.fn), static_cast<long long>(p.smem), g.KC, g.s, g.J,
                                 g.b, g.out_mode, g.stages, g.stage_bytes, g.a_block_bytes, g.b_block_bytes,
-                                g.b_pad_lo_bytes, g.b_region_bytes, g.tmem_cols, g.n_acc, g.n_iss, g.G};
+                                g.b_pad_lo_bytes, g.b_region_bytes, g.tmem_cols, g.n_acc, g.n_iss, g.G, g.dbl_mask};
     for (long long x : head) f.v[f.n++] = x;
     for (int a = 0; a < kMaxAcc; ++a) f.v[f.n++] = g.acc_t0[a];
     for (int i = 0; i < g.G; ++i)
-        for (long long x : {g.blk_lo[i], g.blk_nb[i], g.blk_p0[i], g.blk_p1[i], g.blk_period[i], g.blk_off[i]})
+        for (long long x : {g.blk_lo[i], g.blk_nb[i], g.blk_p0[i], g.blk_p1[i], g.blk_period[i], g.blk_off[i],
+                            g.blk_col1[i]})
             f.v[f.n++] = x;
     unsigned long long h = 1469598103934665603ull;  // FNV-1a over the words
     for (int i = 0; i < f.n; ++i) h = (h ^ static_cast<unsigned long long>(f.v[i])) * 1099511628211ull;
@@ -1088,6 +1098,7 @@ void fill_blocks(const Plan &p, ozgb_config *out) {
     out->umma_per_kstep = p.mma_per_kstep;
     out->issuers = p.n_iss;
     out->slice_format = p.f8 ? 1 : 0;
+    out->dbl_blocks = static_cast<int>(p.dbl_mask);
     for (int i = 0; i < 8; ++i) {
         out->block_lo[i] = i < p.G ? p.blk_lo[i] : 0;
         out->block_nb[i] = i < p.G ? p.blk_nb[i] : 0;
@@ -1308,6 +1319,24 @@ ozgb_status ozgb_set_slice_format(ozgb_handle h, int format) {
     if (!h || format < 0 || format > 1) return OZGB_ERR_ARG;
     std::lock_guard<std::mutex> lk(h->mu);
     h->opt_format = format;
+    return OZGB_OK;
+}
+ozgb_status ozgb_set_plan_hint(ozgb_handle h, int tile_n, int k_chunk, int stages, int issuers, int dbl, int blocks,
+                               const int *block_nb) {
+    if (!h || tile_n < 0 || k_chunk < 0 || stages < 0 || issuers < 0 || issuers > kMaxIssuers || dbl < -1 ||
+        dbl > 1 || blocks < 0 || blocks > kMaxGroups || (blocks > 0 && !block_nb))
+        return OZGB_ERR_ARG;
+    std::lock_guard<std::mutex> lk(h->mu);
+    PlanHints ph;
+    ph.BN = tile_n;
+    ph.KC = k_chunk;
+    ph.stages = stages;
+    ph.issuers = issuers;
+    ph.dbl = dbl;
+    ph.groups = blocks;
+    for (int i = 0; i < blocks; ++i) ph.sizes[i] = block_nb[i];
+    h->plan_hint = ph;
+    h->have_plan_hint = tile_n || k_chunk || stages || issuers || dbl != -1 || blocks;
     return OZGB_OK;
 }
 ozgb_status ozgb_set_error_bound(ozgb_handle h, double bound) {

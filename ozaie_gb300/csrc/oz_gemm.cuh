@@ -361,9 +361,6 @@ __device__ __forceinline__ void tile_ref(const GemmArgs &g, int u, TileRef *r) {
     r->b_src = reinterpret_cast<const uint8_t *>(g.b_tiles) + static_cast<size_t>(r->nt) * g.n_kc * g.b_block_bytes;
 }
 
-// Stage mask value that ends the MMA issuer's loop (after the CTA's last tile).
-constexpr uint32_t kStageTerminate = 0x80000000u;
-
 // Persistent: CTA b processes tiles b, b + gridDim.x, ...  The stage ring, the
 // bin-block barriers and TMEM persist across tiles, so the producer prefetches
 // the next tile's first chunks and the UMMAs of the next tile start as soon as
@@ -383,22 +380,16 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + static_cast<size_t>(g.stages) * g.stage_bytes);
     uint64_t *empty = full + g.stages;
     uint64_t *gfull = empty + g.stages;
-    uint64_t *gempty = gfull + kMaxGroups;
-    uint64_t *mma_done = gempty + kMaxGroups;
+    uint64_t *gempty = gfull + 2 * kMaxGroups;  // [block][buffer]: index 2 * blk + buf
+    uint64_t *mma_done = gempty + 2 * kMaxGroups;
     uint64_t *split_bar = mma_done + 1;  // the drain warps' barrier around a split tile's count
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(split_bar + 1);
     int *abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
     volatile int *vabort = abort_flag;
-    // drain mask of the chunk held by each stage (written by the producer before it
-    // arms the stage), and the per-block UMMA parameters of the issuer
-    uint32_t *stage_mask = reinterpret_cast<uint32_t *>(abort_flag + 1);  // [stages <= 8]
-    uint64_t *blk_ad = reinterpret_cast<uint64_t *>(
-        (reinterpret_cast<uintptr_t>(stage_mask + 8) + 7) & ~uintptr_t(7));  // [kMaxGroups]
-    uint64_t *blk_bd = blk_ad + kMaxGroups;
-    uint32_t *blk_tm = reinterpret_cast<uint32_t *>(blk_bd + kMaxGroups);   // TMEM address
-    uint32_t *blk_id = blk_tm + kMaxGroups;                                 // instruction descriptor
-    int *blk_np = reinterpret_cast<int *>(blk_id + kMaxGroups);             // A slices per UMMA run
-    int *split_flag = blk_np + kMaxGroups;  // this CTA's part completed a split tile
+    // the drain warps' block table: TMEM column of bin lo of block g in buffer b
+    // at [2 g + b], then lo at [2 kMaxGroups + g] and nb at [3 kMaxGroups + g]
+    int *drn = abort_flag + 1;
+    int *split_flag = drn + 4 * kMaxGroups;  // this CTA's part completed a split tile
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -415,18 +406,30 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
-    const int n_iss = (g.G >= 2 && g.n_iss >= 2) ? 2 : 1;  // MMA-issuing threads (blocks split by parity)
+    const int n_iss = g.n_iss < 1 ? 1 : (g.n_iss > kMaxIssuers ? kMaxIssuers : g.n_iss);  // MMA-issuing warps
     if (threadIdx.x == 0) {
         for (int i = 0; i < g.stages; ++i) {
             mbar_init(&full[i], 1);
             mbar_init(&empty[i], n_iss);
         }
+        // a block's drain waits for every issuer that has runs in it: its runs are
+        // consecutive run numbers, so min(runs, n_iss) issuers
         for (int i = 0; i < g.G; ++i) {
-            mbar_init(&gfull[i], 1);
-            mbar_init(&gempty[i], kEpiWarps);
+            const int runs = g.blk_p1[i] - g.blk_p0[i] + 1;
+            const int contributors = runs < n_iss ? runs : n_iss;
+            for (int b = 0; b < 2; ++b) {
+                mbar_init(&gfull[2 * i + b], contributors);
+                mbar_init(&gempty[2 * i + b], kEpiWarps);
+            }
         }
         mbar_init(mma_done, n_iss);
         mbar_init(split_bar, kEpiWarps);
+        for (int i = 0; i < g.G; ++i) {
+            drn[2 * i] = g.blk_lo[i] * BN;
+            drn[2 * i + 1] = ((g.dbl_mask >> i) & 1u) ? g.blk_col1[i] : g.blk_lo[i] * BN;
+            drn[2 * kMaxGroups + i] = g.blk_lo[i];
+            drn[3 * kMaxGroups + i] = g.blk_nb[i];
+        }
         *abort_flag = (*reinterpret_cast<volatile int *>(g.err) != 0) ? 1 : 0;
         fence_mbar_init();
     }
@@ -439,6 +442,17 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
     const uint64_t TO = g.timeout_ns;
+    // Every UMMA accumulates, so TMEM starts zeroed (and each drain leaves what it
+    // read zeroed): drain warp (quadrant qd, part) clears its quarter of the columns.
+    if (warp >= 2 && warp < 2 + kEpiWarps) {
+        const uint32_t quarter = g.tmem_cols >> 2;
+        const uint32_t base = tmem + (static_cast<uint32_t>(32 * (warp & 3)) << 16) + ((warp - 2) >> 2) * quarter;
+        for (uint32_t col = 0; col < quarter; col += 8) tmem_st8_zero(base + col);
+        tmem_st_wait();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
 
     if (warp == 0) {
         // ------------------------------------------------------ producer
@@ -460,15 +474,12 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
             for (int t = g.tile_begin + static_cast<int>(blockIdx.x); ok && t < g.total_tiles; t += gridDim.x) {
                 TileRef tr;
                 tile_ref(g, t, &tr);
-                DrainSchedule pds;
-                pds.init(g);
                 for (int c = tr.c0; c < tr.c1; ++c) {
                     if (*vabort || !acquire()) {
                         ok = false;
                         break;
                     }
                     uint8_t *dst = smem + static_cast<size_t>(st) * g.stage_bytes;
-                    stage_mask[st] = pds.next(g, c == tr.c1 - 1);  // published by the arrive below
                     mbar_arrive_expect_tx(&full[st], g.a_block_bytes + g.b_block_bytes);
                     bulk_g2s(dst, tr.a_src + static_cast<size_t>(c) * g.a_block_bytes, g.a_block_bytes, &full[st]);
                     bulk_g2s(dst + g.a_block_bytes + g.b_pad_lo_bytes,
@@ -477,131 +488,149 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                     if (++st == g.stages) st = 0;
                 }
             }
-            // end of work: one more stage use, without copies, tells the MMA issuer to stop
-            bool posted = false;
-            if (ok && !*vabort && acquire()) {
-                stage_mask[st] = kStageTerminate;
-                mbar_arrive(&full[st]);
-                posted = true;
-            }
-            // every copy issued must land before the CTA may exit (a stage reused by
-            // the terminate signal was consumed, so its copies have landed)
+            // every copy issued must land before the CTA may exit
             const int zero = 0;
-            const long long first = issued - g.stages + (posted ? 1 : 0);
+            const long long first = issued - g.stages;
             for (long long c = (first > 0 ? first : 0); c < issued; ++c)
                 mbar_wait(&full[c % g.stages], static_cast<uint32_t>((c / g.stages) & 1), &zero, TO);
         }
-    } else if (warp == 1 || warp == kIssuer2Warp) {
+    } else if (warp == 1 || warp >= kIssuer2Warp) {
         // ---------------------------------------------------- MMA issuers
-        // Issuer iss issues the UMMAs of the bin blocks blk with blk % n_iss == iss
-        // and commits every stage it has read to the stage's empty barrier.
-        const int iss = warp == 1 ? 0 : 1;
-        if (lane == 0 && iss < n_iss) {
-            uint32_t mine = 0;
-            for (int i = 0; i < g.G; ++i)
-                if (i % n_iss == iss) mine |= 1u << i;
+        // Up to three issuing warps (on different SM sub-partitions), each run warp-wide
+        // with lane 0 issuing and committing.  The UMMA runs of a K step (block g,
+        // A slice p: ksteps UMMAs) are numbered block by block and dealt round-robin:
+        // issuer iss takes the runs r with r % n_iss == iss.  Every UMMA accumulates
+        // (the drain warps leave the accumulators they read out zeroed), so the
+        // issuers of one block need no ordering among themselves.
+        const int iss = warp == 1 ? 0 : warp - kIssuer2Warp + 1;
+        if (iss < n_iss) {
             constexpr uint32_t a_step = (BM * KC * 2) >> 4;  // descriptor units (16 B)
             constexpr uint32_t b_step = (BN * KC * 2) >> 4;
             constexpr uint32_t sbo = KC * 16;
             constexpr int ksteps = KC >> 4;
-            {
-                // per-block UMMA parameters, once: every scalar instruction of the issuing
-                // thread between UMMAs can leave the tensor core idle
-                const uint32_t a0 = smem_u32(smem);
-                const uint64_t ad0 = smem_desc(a0, 128, sbo);
-                const uint64_t bd0 = smem_desc(a0 + g.a_block_bytes + g.b_pad_lo_bytes, 128, sbo);
-                const uint32_t idesc_base = (F8 ? idesc_e4m3_f32(BM, 16) : idesc_bf16_f32(BM, 16)) & ~(0x3Fu << 17);
+            const uint32_t a0 = smem_u32(smem);
+            const uint64_t ad0 = smem_desc(a0, 128, sbo);
+            const uint64_t bd0 = smem_desc(a0 + g.a_block_bytes + g.b_pad_lo_bytes, 128, sbo);
+            const uint32_t idesc_base = (F8 ? idesc_e4m3_f32(BM, 16) : idesc_bf16_f32(BM, 16)) & ~(0x3Fu << 17);
+            // block table in the lanes (lane i: block i): bins, A slices, second buffer,
+            // and this issuer's first A slice in the block (> p1: no runs there)
+            int t_lo = 0, t_nb = 0, t_p0 = 0, t_p1 = -1, t_c1 = 0;
 #pragma unroll
-                for (int i = 0; i < kMaxGroups; ++i) {
-                    if (i < g.G && ((mine >> i) & 1u)) {
-                        blk_ad[i] = ad0 + static_cast<uint64_t>(g.blk_p0[i]) * a_step;
-                        blk_bd[i] = bd0 + static_cast<uint64_t>(static_cast<int64_t>(g.blk_lo[i] - g.blk_p0[i]) * b_step);
-                        blk_tm[i] = tmem + static_cast<uint32_t>(g.blk_lo[i] * BN);
-                        blk_id[i] = idesc_base | (static_cast<uint32_t>((g.blk_nb[i] * BN) >> 3) << 17);
-                        blk_np[i] = g.blk_p1[i] - g.blk_p0[i] + 1;
-                    }
+            for (int i = 0; i < kMaxGroups; ++i)
+                if (lane == i && i < g.G) {
+                    t_lo = g.blk_lo[i];
+                    t_nb = g.blk_nb[i];
+                    t_p0 = g.blk_p0[i];
+                    t_p1 = g.blk_p1[i];
+                    t_c1 = g.blk_col1[i];
                 }
+            const int runs = t_p1 - t_p0 + 1;
+            int incl = runs;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, off);
+                if (lane >= off) incl += y;
             }
-            const uint32_t all = mine;
-            uint64_t ephase = 0;            // per-block parity of gempty waits
-            uint32_t prev = 0;              // blocks drained after the previous chunk (of any tile)
-            uint32_t fresh = all;           // blocks whose next UMMA overwrites the accumulators
+            const int rb = incl - runs;  // runs of the blocks before this one
+            const int t_pf = t_p0 + ((iss - rb % n_iss) % n_iss + n_iss) % n_iss;
+            const uint32_t mine = __ballot_sync(0xffffffffu, lane < g.G && t_pf <= t_p1);
+            const uint32_t dbl = g.dbl_mask & mine;  // double-buffered: UMMAs go on during their drains
+            uint32_t ephase = 0;  // parity of the gempty waits, bit 2 blk + buf
+            uint32_t pend = 0;    // drains committed and not yet waited for, bit 2 blk + buf
+            uint32_t bufm = 0;    // accumulator buffer each block writes now
+            uint32_t prev = 0;    // single-buffered blocks drained after the previous chunk
             int st = 0;
             uint32_t fparity = 0;
             bool ok = true;
-            for (;;) {
-                const bool gotf = mbar_wait(&full[st], fparity, vabort, TO);
-                if (!gotf) {
-                    ok = false;
-                    break;
-                }
-                tc_fence_after();
-                const uint64_t stage_off = (static_cast<uint64_t>(st) * g.stage_bytes) >> 4;
-                const uint32_t cur = stage_mask[st];
-                if (cur & kStageTerminate) break;
-                // issue order: blocks drained after this chunk, then the rest, then the
-                // blocks whose drain (after the previous chunk) must finish first
-                uint32_t order[3] = {cur & all & ~prev, all & ~cur & ~prev, prev};
-                for (int cls = 0; ok && cls < 3; ++cls) {
-                    uint32_t m = order[cls];
-                    while (m) {
-                        const int blk = __ffs(m) - 1;
-                        const uint32_t bit = 1u << blk;
-                        m &= m - 1;
-                        if (cls == 2) {
-                            const bool gote = mbar_wait(&gempty[blk],
-                                                        static_cast<uint32_t>((ephase >> blk) & 1ull), vabort, TO);
-                            if (!gote) {
-                                ok = false;
-                                break;
+            for (int t = g.tile_begin + static_cast<int>(blockIdx.x); ok && t < g.total_tiles; t += gridDim.x) {
+                TileRef tr;
+                tile_ref(g, t, &tr);
+                DrainSchedule ds;
+                ds.init(g);
+                for (int c = tr.c0; c < tr.c1; ++c) {
+                    const uint32_t cur = ds.next(g, c == tr.c1 - 1);
+                    int got = 1;
+                    if (lane == 0) got = mbar_wait(&full[st], fparity, vabort, TO) ? 1 : 0;
+                    if (!__shfl_sync(0xffffffffu, got, 0)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint64_t stage_off = (static_cast<uint64_t>(st) * g.stage_bytes) >> 4;
+                    // issue order: blocks drained after this chunk, then the rest, then the
+                    // blocks whose drain (after the previous chunk) must finish first
+                    const uint32_t order[3] = {cur & mine & ~prev, mine & ~cur & ~prev, prev};
+                    for (int cls = 0; ok && cls < 3; ++cls) {
+                        uint32_t m = order[cls];
+                        while (m) {
+                            const int blk = __ffs(m) - 1;
+                            const uint32_t bit = 1u << blk;
+                            m &= m - 1;
+                            const int lo = __shfl_sync(0xffffffffu, t_lo, blk);
+                            const int nb = __shfl_sync(0xffffffffu, t_nb, blk);
+                            const int p1 = __shfl_sync(0xffffffffu, t_p1, blk);
+                            const int pf = __shfl_sync(0xffffffffu, t_pf, blk);
+                            const int c1 = __shfl_sync(0xffffffffu, t_c1, blk);
+                            const int bb = static_cast<int>((bufm >> blk) & 1u);
+                            const int ix = 2 * blk + bb;
+                            if ((pend >> ix) & 1u) {
+                                // the buffer's previous drain must have read it out
+                                int gote = 1;
+                                if (lane == 0) gote = mbar_wait(&gempty[ix], (ephase >> ix) & 1u, vabort, TO) ? 1 : 0;
+                                if (!__shfl_sync(0xffffffffu, gote, 0)) {
+                                    ok = false;
+                                    break;
+                                }
+                                ephase ^= 1u << ix;
+                                pend &= ~(1u << ix);
+                                tc_fence_after();
                             }
-                            ephase ^= (1ull << blk);
-                            tc_fence_after();
-                        }
-                        const uint32_t d_tmem = blk_tm[blk];
-                        const uint32_t idesc = blk_id[blk];
-                        const int np = blk_np[blk];
-                        uint64_t ad = blk_ad[blk] + stage_off;
-                        uint64_t bd = blk_bd[blk] + stage_off;
-                        uint32_t acc = (fresh & bit) ? 0u : 1u;
-                        for (int p = 0; p < np; ++p) {
+                            const uint32_t d_tmem = tmem + static_cast<uint32_t>(bb ? c1 : lo * BN);
+                            const uint32_t idesc = idesc_base | (static_cast<uint32_t>((nb * BN) >> 3) << 17);
+                            for (int p = pf; p <= p1; p += n_iss) {
+                                // A slice p against B slices q = j - p of the block's bins j
+                                const uint64_t ad = ad0 + stage_off + static_cast<uint64_t>(p) * a_step;
+                                const uint64_t bd =
+                                    bd0 + stage_off + static_cast<uint64_t>(static_cast<int64_t>(lo - p) * b_step);
+                                if (lane == 0) {
 #pragma unroll
-                            for (int kk = 0; kk < ksteps; ++kk) {
-                                // one UMMA covers 32 bytes of K per row: 16 bf16 or 32 e4m3 values
-                                if constexpr (F8)
-                                    umma_e4m3(d_tmem, ad + static_cast<uint64_t>(kk * 16),
-                                              bd + static_cast<uint64_t>(kk * 16), idesc, acc);
-                                else
-                                    umma_bf16(d_tmem, ad + static_cast<uint64_t>(kk * 16),
-                                              bd + static_cast<uint64_t>(kk * 16), idesc, acc);
-                                acc = 1u;
+                                    for (int kk = 0; kk < ksteps; ++kk) {
+                                        // one UMMA covers 32 bytes of K per row: 16 bf16 or 32 e4m3 values
+                                        if constexpr (F8)
+                                            umma_e4m3(d_tmem, ad + static_cast<uint64_t>(kk * 16),
+                                                      bd + static_cast<uint64_t>(kk * 16), idesc, 1u);
+                                        else
+                                            umma_bf16(d_tmem, ad + static_cast<uint64_t>(kk * 16),
+                                                      bd + static_cast<uint64_t>(kk * 16), idesc, 1u);
+                                    }
+                                }
                             }
-                            ad += a_step;
-                            bd -= b_step;
-                        }
-                        fresh &= ~bit;
-                        if (cur & bit) {
-                            umma_commit(&gfull[blk]);
-                            fresh |= bit;
+                            if (cur & bit) {
+                                if (lane == 0) umma_commit(&gfull[ix]);
+                                pend |= 1u << ix;
+                                if (dbl & bit) bufm ^= bit;
+                            }
                         }
                     }
+                    if (!ok) break;
+                    if (lane == 0) umma_commit(&empty[st]);
+                    if (++st == g.stages) {
+                        st = 0;
+                        fparity ^= 1u;
+                    }
+                    prev = cur & mine & ~dbl;
                 }
-                if (!ok) break;
-                umma_commit(&empty[st]);
-                if (++st == g.stages) {
-                    st = 0;
-                    fparity ^= 1u;
-                }
-                prev = cur & all;
             }
-            if (!ok && !*vabort) {
+            if (!ok && lane == 0 && !*vabort) {
                 atomicCAS(g.err, 0, DEVERR_TIMEOUT_MMA);
                 *vabort = 1;
             }
-            // all MMAs issued by this thread complete before TMEM is released
-            umma_commit(mma_done);
-            const int zero = 0;
-            mbar_wait(mma_done, 0, &zero, TO);
+            // all MMAs issued by this warp complete before TMEM is released
+            if (lane == 0) {
+                umma_commit(mma_done);
+                const int zero = 0;
+                mbar_wait(mma_done, 0, &zero, TO);
+            }
         }
         __syncwarp();
     } else {
@@ -612,7 +641,8 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
         const uint32_t trow = tmem + (static_cast<uint32_t>(32 * qd) << 16) + static_cast<uint32_t>(part * COLS);
 
         long long acc[COLS][NA];
-        uint64_t fphase = 0;
+        uint32_t fphase = 0;  // parity of the gfull waits, bit 2 blk + buf
+        uint32_t dbuf = 0;    // accumulator buffer each block's next drain reads
         uint32_t prev = 0;
         bool ok = true;
         // barrier of the 16 drain warps (one arrival per warp), with the bounded wait
@@ -643,22 +673,19 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
                     while (m) {
                         const int blk = __ffs(m) - 1;
                         m &= m - 1;
-                        const bool gotg =
-                            mbar_wait(&gfull[blk], static_cast<uint32_t>((fphase >> blk) & 1ull), vabort, TO);
+                        const int bb = static_cast<int>((dbuf >> blk) & 1u);
+                        const int ix = 2 * blk + bb;
+                        const bool gotg = mbar_wait(&gfull[ix], (fphase >> ix) & 1u, vabort, TO);
                         if (!gotg) {
                             ok = false;
                             break;
                         }
-                        fphase ^= (1ull << blk);
+                        fphase ^= 1u << ix;
                         tc_fence_after();
-                        int lo = 0, nb = 0;  // static-index selects (see the MMA issuer)
-#pragma unroll
-                        for (int i = 0; i < kMaxGroups; ++i)
-                            if (i == blk) {
-                                lo = g.blk_lo[i];
-                                nb = g.blk_nb[i];
-                            }
-                        const int hi = lo + nb - 1;
+                        const int lo = drn[2 * kMaxGroups + blk];
+                        const int hi = lo + drn[3 * kMaxGroups + blk] - 1;
+                        // bin j of the buffer read is at column drn[ix] + (j - lo) BN
+                        const uint32_t bbase = trow + static_cast<uint32_t>(drn[ix] - lo * BN);
                         for (int j = lo; j <= hi; ++j) {
                             // accumulator group of bin j and its weight within the group
                             const int t = g.J - 1 - j;
@@ -673,20 +700,24 @@ __global__ void __launch_bounds__(kThreads, 1) oz_gemm_kernel(const __grid_const
 #pragma unroll
                             for (int cb = 0; cb < COLS / DB; ++cb) {
                                 uint32_t v[DB];
-                                tmem_ld_cols<DB>(trow + j * BN + cb * DB, v);
+                                const uint32_t taddr = bbase + static_cast<uint32_t>(j * BN + cb * DB);
+                                tmem_ld_cols<DB>(taddr, v);
                                 tmem_ld_wait();
+                                tmem_zero_cols<DB>(taddr);  // the next UMMAs accumulate onto zero
 #pragma unroll
                                 for (int i = 0; i < DB; ++i) reg_fence(v[i]);
                                 acc_add_group<NA, DB>(acc + cb * DB, v, a, rel);
                             }
                         }
-                        // the block's accumulators are free for the next chunk (or tile)
+                        // the buffer is zeroed and free for the block's UMMAs again
+                        tmem_st_wait();
                         tc_fence_before();
                         __syncwarp();
-                        if (lane == 0) mbar_arrive(&gempty[blk]);
+                        if (lane == 0) mbar_arrive(&gempty[ix]);
+                        if ((g.dbl_mask >> blk) & 1u) dbuf ^= 1u << blk;
                     }
                 }
-                prev = cur;
+                prev = cur & ~g.dbl_mask;
             }
             if (!ok) break;
 

@@ -25,11 +25,14 @@ constexpr int kMaxBins = 64;      // J limit
 constexpr int kMaxGroups = 8;     // drain groups limit
 constexpr int kMaxAcc = 4;        // 64-bit accumulator groups per element (drain)
 constexpr int kEpiWarps = 16;     // drain + epilogue warps: 4 per TMEM lane quadrant
-// warp 0 producer, warp 1 MMA issuer, then the drain warps, then a second MMA
-// issuer (on another scheduler than the first: the bin blocks are split between
-// the two so neither issuing thread's instruction stream limits the tensor pipe)
-constexpr int kThreads = 64 + 32 * kEpiWarps + 32;
-constexpr int kIssuer2Warp = 2 + kEpiWarps;
+// warp 0 producer, warp 1 MMA issuer, then the drain warps, then two more MMA
+// issuers, so that the issuing warps sit on three different schedulers: one thread
+// issues a UMMA about every 80-100 SM cycles, while the tensor pipe takes N / 2
+// cycles for one of N columns, so narrow UMMAs need several issuers to keep it
+// busy.  (640 threads keep ptxas's register limit at 96 per thread.)
+constexpr int kThreads = 64 + 32 * kEpiWarps + 64;
+constexpr int kIssuer2Warp = 2 + kEpiWarps;  // issuing warps: 1, kIssuer2Warp and kIssuer2Warp + 1
+constexpr int kMaxIssuers = 3;
 constexpr int kMaxAccWords = 5;
 
 // OUT_PAIRS writes the reference's device output (its C buffer before the host
@@ -91,6 +94,11 @@ struct GemmArgs {
     int G;
     int blk_lo[kMaxGroups], blk_nb[kMaxGroups], blk_p0[kMaxGroups], blk_p1[kMaxGroups];
     int blk_period[kMaxGroups], blk_off[kMaxGroups];
+    // Double-buffered blocks (bit g of dbl_mask): a second accumulator range at
+    // TMEM column blk_col1[g]; after each drain the block's UMMAs switch ranges,
+    // so they go on while the drain warps read the other one out.
+    uint32_t dbl_mask;
+    int blk_col1[kMaxGroups];
     int total_tiles;  // end of the launch's tile range (tiles_m * tiles_n for the whole product)
     int tile_begin;   // first tile of the launch's range (0 for the whole product)
     // Grouped launch (null otherwise): work unit u < total_tiles is tile
@@ -177,7 +185,8 @@ typedef void (*GemmLaunchFn)(const GemmArgs &args, int grid, size_t smem, void *
 // first; defined in oz_gemm_v*.cu.
 #define OZ_GEMM_VARIANTS(X)                                                                        \
     X(128, 2, 32) X(128, 2, 16) X(64, 3, 32) X(64, 3, 16) X(64, 4, 32) X(64, 4, 16) X(48, 3, 32)   \
-    X(48, 3, 16) X(48, 4, 32) X(48, 4, 16) X(32, 4, 32) X(32, 4, 16) X(32, 5, 32) X(32, 5, 16)     \
+    X(48, 3, 16) X(48, 4, 32) X(48, 4, 16) X(32, 3, 32) X(32, 3, 16) X(32, 4, 32) X(32, 4, 16)     \
+    X(32, 5, 32) X(32, 5, 16)                                                                       \
     X(16, 4, 32) X(16, 4, 16) X(16, 5, 32) X(16, 5, 16)
 #define OZ_DECLARE_GEMM(BN, W, KC) void launch_gemm_##BN##_##W##_##KC(const GemmArgs &, int, size_t, void *);
 OZ_GEMM_VARIANTS(OZ_DECLARE_GEMM)

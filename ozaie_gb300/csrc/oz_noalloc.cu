@@ -167,7 +167,9 @@ extern "C" ozgb_status ozgb_dgemm_device_noalloc(int M, int N, int K, const doub
         g.blk_p1[i] = p.blk_p1[i];
         g.blk_period[i] = p.blk_period[i];
         g.blk_off[i] = p.blk_off[i];
+        g.blk_col1[i] = p.blk_col1[i];
     }
+    g.dbl_mask = p.dbl_mask;
     p.fn(g, p.tiles_m * p.tiles_n, p.smem, st);
     if (cudaGetLastError() != cudaSuccess) return OZGB_ERR_EXEC;  // the slice-pair GEMM launch
     return OZGB_OK;

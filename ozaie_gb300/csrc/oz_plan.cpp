@@ -402,8 +402,11 @@ bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std
         p.pad_hi = std::max(p.pad_hi, hi - p.blk_p0[g] - (s - 1));  // q = hi - p0 <= s - 1 + pad_hi
     }
 
-    // two issuing threads (bin blocks split by parity) unless the hint says one
-    p.n_iss = (p.G >= 2 && hint.issuers != 1) ? 2 : 1;
+    // issuing warps (1 to 3; the UMMA runs of a K step are dealt round-robin): one
+    // warp issues a UMMA about every 80-100 SM cycles and the tensor pipe takes
+    // N / 2 cycles for N columns, so three unless there are fewer runs than that
+    p.n_iss = hint.issuers >= 1 && hint.issuers <= kMaxIssuers ? hint.issuers : kMaxIssuers;
+    p.n_iss = std::min(p.n_iss, std::max(1, p.mma_per_kstep));
 
     // ---- pipeline: K chunk and stage count (a chunk of 32 bf16 or 64 e4m3 K values
     // is 64 bytes per row and slice)
@@ -483,8 +486,35 @@ bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std
     p.b_elems = static_cast<size_t>(p.tiles_n) * p.n_kc * s * p.BN * p.KC;
     p.a_bytes = p.a_elems * eb;
     p.b_bytes = p.b_elems * eb;
+    // ---- double buffering: blocks get a second accumulator range in the TMEM
+    // columns the bins leave free, most frequently drained blocks first (the
+    // order does not depend on K, so problems of one shape class share a plan);
+    // their UMMAs then switch ranges at each drain, and at the end of a tile,
+    // instead of waiting for the drain warps to read the block out.
+    p.dbl_mask = 0;
+    int next_col = J * p.BN;  // buffer 0: bin j at column j BN
+    if (hint.dbl != 0) {
+        int order[kMaxGroups], n = 0;
+        long period[kMaxGroups];  // in K values, not clamped to this K
+        for (int g = 0; g < p.G; ++g) {
+            order[n++] = g;
+            period[g] = 1L << 40;
+            for (int j = p.blk_lo[g]; j < p.blk_lo[g] + p.blk_nb[g]; ++j)
+                period[g] = std::min(period[g], static_cast<long>(std::floor(16777216.0 / (pairs_in_bin(j, s) * v2 * v2))));
+        }
+        std::sort(order, order + n, [&](int x, int y) {
+            return period[x] != period[y] ? period[x] < period[y] : (p.blk_nb[x] != p.blk_nb[y] ? p.blk_nb[x] > p.blk_nb[y] : x < y);
+        });
+        for (int i = 0; i < n; ++i) {
+            const int g = order[i];
+            if (next_col + p.blk_nb[g] * p.BN > 512) continue;
+            p.dbl_mask |= 1u << g;
+            p.blk_col1[g] = next_col;
+            next_col += p.blk_nb[g] * p.BN;
+        }
+    }
     uint32_t cols = 32;
-    while (cols < static_cast<uint32_t>(J * p.BN)) cols <<= 1;
+    while (cols < static_cast<uint32_t>(next_col)) cols <<= 1;
     p.tmem_cols = cols;
     p.smem = static_cast<size_t>(p.stages) * p.stage_bytes + kCtrlBytes;
     *out = p;
@@ -498,7 +528,7 @@ std::vector<PlanHints> plan_candidates(int M, int N, int K, const OzConfig &cfg,
     std::vector<Plan> plans;
     auto same = [](const Plan &x, const Plan &y) {
         if (x.f8 != y.f8 || x.BN != y.BN || x.KC != y.KC || x.G != y.G || x.stages != y.stages ||
-            x.n_iss != y.n_iss)
+            x.n_iss != y.n_iss || x.dbl_mask != y.dbl_mask)
             return false;
         for (int i = 0; i < x.G; ++i)
             if (x.blk_lo[i] != y.blk_lo[i] || x.blk_nb[i] != y.blk_nb[i]) return false;
@@ -516,17 +546,20 @@ std::vector<PlanHints> plan_candidates(int M, int N, int K, const OzConfig &cfg,
         exact.groups = p.G;
         exact.stages = p.stages;
         exact.issuers = p.n_iss;
+        exact.dbl = p.dbl_mask ? 1 : 0;
         for (int g = 0; g < kMaxGroups; ++g) exact.sizes[g] = g < p.G ? p.blk_nb[g] : 0;
         plans.push_back(p);
         out.push_back(exact);
-        if (p.n_iss == 2 && !h.issuers) {
-            // the same plan with one issuing thread
-            PlanHints one = exact;
-            one.issuers = 1;
-            Plan q;
-            if (make_plan(M, N, K, cfg, &q, &why, 0, 1 << 30, &one)) {
-                plans.push_back(q);
-                out.push_back(one);
+        if (!h.issuers) {
+            // the same plan with fewer issuing warps
+            for (int ni = p.n_iss - 1; ni >= 1; --ni) {
+                PlanHints fewer = exact;
+                fewer.issuers = ni;
+                Plan q;
+                if (make_plan(M, N, K, cfg, &q, &why, 0, 1 << 30, &fewer)) {
+                    plans.push_back(q);
+                    out.push_back(fewer);
+                }
             }
         }
     };

@@ -35,6 +35,8 @@ struct Plan {
     int blk_period[kMaxGroups] = {0}, blk_off[kMaxGroups] = {0};
     int n_acc = 0, acc_t0[kMaxAcc] = {0};  // drain accumulator groups (GemmArgs)
     int n_iss = 1;                         // MMA-issuing threads
+    uint32_t dbl_mask = 0;                 // double-buffered blocks (GemmArgs)
+    int blk_col1[kMaxGroups] = {0};        // their second accumulator range (TMEM column)
     GemmLaunchFn fn = nullptr;
 };
 
@@ -54,6 +56,7 @@ struct PlanHints {
     int sizes[kMaxGroups] = {0};  // explicit bin-block sizes (groups of them), overriding the cost model
     int min_W = 0;                // at least this many accumulator words (4 for OUT_PAIRS)
     int issuers = 0;              // MMA-issuing threads (1 or 2)
+    int dbl = -1;                 // double-buffered blocks: -1 the planner's choice, 0 none, 1 every one that fits
 };
 
 // Builds the plan for bins [bin_lo, bin_hi] of the pair set (the full set of

@@ -140,6 +140,17 @@ __device__ __forceinline__ void tmem_st8_zero(uint32_t taddr) {
         "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%1,%1,%1,%1,%1,%1,%1};" ::"r"(taddr), "r"(z)
         : "memory");
 }
+__device__ __forceinline__ void tmem_st4_zero(uint32_t taddr) {
+    const uint32_t z = 0;
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%1,%1,%1};" ::"r"(taddr), "r"(z) : "memory");
+}
+// Zeroes N consecutive columns (N a multiple of 4) of this warp's 32 TMEM lanes.
+template <int N>
+__device__ __forceinline__ void tmem_zero_cols(uint32_t taddr) {
+#pragma unroll
+    for (int l = 0; l < N / 8; ++l) tmem_st8_zero(taddr + l * 8);
+    if constexpr (N % 8 == 4) tmem_st4_zero(taddr + (N / 8) * 8);
+}
 __device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 // Makes values produced by an asynchronous TMEM load visible as ordinary
 // register dependencies after tmem_ld_wait().
