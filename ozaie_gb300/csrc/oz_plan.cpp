@@ -2,6 +2,7 @@
 #include "oz_plan.h"
 
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <cstdlib>
 #include <map>
@@ -254,124 +255,89 @@ bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std
     for (int a = 0; a < kMaxAcc; ++a) p.acc_t0[a] = acc_t0[a];
 
     // ---- bin blocks: contiguous bin ranges of at most 256 columns; every UMMA of a
-    // block spans the whole block (zero B slices pad the out-of-range q).  Measured
-    // on GB300 with back-to-back UMMAs (tests/perf/umma_cost.cu): a cta_group::1
-    // UMMA costs a floor of about 140-155 SM cycles whatever its N up to about 200,
-    // its M (64 or 128) or its kind (f16 or f8f6f4), and about 0.66 cycles per
-    // column above that (160-170 at N = 256), so the partition minimising
-    // sum(#A slices x cost(N)), nearly the UMMA count, is chosen by dynamic programming.
+    // block spans the whole block (zero B slices pad the out-of-range q).  Cost of
+    // a partition per 16-deep K step of a tile, in SM cycles, fitted to GB300
+    // measurements of the kernel (three issuing warps, tests/perf/umma_cost.cu for
+    // the UMMA itself): each UMMA N / 2 + 20 (the tensor pipe takes half a cycle per
+    // column; the A tile is re-read from shared memory for every UMMA), each block
+    // 200 (per-block issue work), and for each block the part of its drain (500 +
+    // 800 per 48 columns: the F2I conversions run at 16 per cycle per SM) that two
+    // K steps of the other blocks' UMMAs do not cover, once per drain period.  The
+    // search enumerates the compositions of the bins into G <= 8 blocks whose sizes
+    // stay within one of the even split, for every G.
     const int max_groups = kMaxGroups;
     const int maxb = 256 / p.BN;
+    const int kpu = p.f8 ? 32 : 16;  // K values per UMMA
     auto p0_of = [s](int lo) { return std::max(0, lo - (s - 1)); };
     auto p1_of = [s](int hi) { return std::min(hi, s - 1); };
-    auto blk_cost = [&](int lo, int hi) {
-        const int nops = p1_of(hi) - p0_of(lo) + 1;
-        return nops * std::max(150.0, 0.66 * (hi - lo + 1) * p.BN);
+    auto period_k = [&](int lo, int nb) {  // K values a block accumulates between drains
+        long kb = 1L << 40;
+        for (int j = lo; j < lo + nb; ++j)
+            if (pairs_in_bin(j, s) > 0)
+                kb = std::min(kb, static_cast<long>(std::floor(16777216.0 / (pairs_in_bin(j, s) * v2 * v2))));
+        const long chunk = 2L * kpu;  // a pipeline chunk holds two UMMA K steps
+        return std::max(chunk, (kb / chunk) * chunk);
+    };
+    auto part_cost = [&](int G, const int *lo, const int *nb) {
+        double t[kMaxGroups], T = 200.0 * G;
+        for (int g = 0; g < G; ++g) {
+            const int runs = p1_of(lo[g] + nb[g] - 1) - p0_of(lo[g]) + 1;
+            t[g] = runs * (0.5 * nb[g] * p.BN + 20.0);
+            T += t[g];
+        }
+        double stall = 0.0;
+        for (int g = 0; g < G; ++g) {
+            const double drain = 500.0 + 800.0 * nb[g] * p.BN / 48.0;
+            stall += std::max(0.0, drain - 2.0 * (T - t[g])) * kpu / static_cast<double>(period_k(lo[g], nb[g]));
+        }
+        return T + stall;
     };
     const int nbins = B1 - B0 + 1;
-    const double INF = 1e300;
-    // best[g][i]: min cost covering bins B0 .. B0+i-1 with g blocks
-    std::vector<std::vector<double>> best(max_groups + 1, std::vector<double>(nbins + 1, INF));
-    std::vector<std::vector<int>> from(max_groups + 1, std::vector<int>(nbins + 1, -1));
-    best[0][0] = 0.0;
-    for (int g = 1; g <= max_groups; ++g)
-        for (int i = 1; i <= nbins; ++i)
-            for (int k = std::max(0, i - maxb); k < i; ++k) {
-                if (best[g - 1][k] >= INF) continue;
-                const double c = best[g - 1][k] + blk_cost(B0 + k, B0 + i - 1);
-                if (c < best[g][i]) {
-                    best[g][i] = c;
-                    from[g][i] = k;
+    double best_cost = HUGE_VAL;
+    int best_G = 0, best_nb[kMaxGroups] = {0};
+    const bool explicit_sizes = hint.groups && hint.sizes[0] > 0;
+    if (!explicit_sizes) {
+        int nb[kMaxGroups], lo[kMaxGroups];
+        // sizes of block g .. G-1 for bins at .. B1, each in [smin, smax]
+        std::function<void(int, int, int, int, int)> rec = [&](int g, int at, int G, int smin, int smax) {
+            if (g == G) {
+                if (at != B1 + 1) return;
+                const double c = part_cost(G, lo, nb);
+                if (c < best_cost - 1e-9) {
+                    best_cost = c;
+                    best_G = G;
+                    for (int i = 0; i < G; ++i) best_nb[i] = nb[i];
                 }
+                return;
             }
-    int gbest = -1;
-    for (int g = 1; g <= max_groups; ++g) {
-        if (hint.groups && g != hint.groups) continue;
-        if (best[g][nbins] < INF && (gbest < 0 || best[g][nbins] < best[gbest][nbins] - 1e-9)) gbest = g;
+            const int left = B1 + 1 - at, rest = G - g - 1;
+            for (int sz = smin; sz <= smax; ++sz) {
+                if (sz > left || left - sz < rest * smin || left - sz > rest * smax) continue;
+                lo[g] = at;
+                nb[g] = sz;
+                rec(g + 1, at + sz, G, smin, smax);
+            }
+        };
+        for (int G = 1; G <= std::min(max_groups, nbins); ++G) {
+            if (hint.groups && G != hint.groups) continue;
+            if ((nbins + G - 1) / G > maxb) continue;
+            const int smin = std::max(1, nbins / G - 1), smax = std::min(maxb, (nbins + G - 1) / G + 1);
+            rec(0, B0, G, smin, smax);
+        }
     }
-    if (gbest < 0) {
+    if (!best_G && !explicit_sizes) {
         *err = "bins do not fit " + std::to_string(max_groups) + " blocks of at most 256 columns";
         return false;
     }
-    p.model_cycles_per_kstep = best[gbest][nbins];
-    p.G = gbest;
-    {
-        int i = nbins;
-        for (int g = gbest; g >= 1; --g) {
-            const int k = from[g][i];
-            p.blk_lo[g - 1] = B0 + k;
-            p.blk_nb[g - 1] = i - k;
-            i = k;
-        }
+    p.G = best_G;
+    p.model_cycles_per_kstep = best_cost;
+    for (int g = 0, at = B0; g < p.G; at += best_nb[g], ++g) {
+        p.blk_lo[g] = at;
+        p.blk_nb[g] = best_nb[g];
     }
-    if (!hint.groups) {
-        // Drain-aware choice among the cost model's best partition per block count
-        // and every two-block split.  A block drained after a chunk must be read out
-        // (about 0.1 SM cycles per value: 16 F2I conversions per cycle) before its
-        // next UMMA; the other blocks' UMMAs of that chunk and the next one cover
-        // the read-out, and what they do not cover stalls the tensor pipe once per
-        // drain period.  Modelled per chunk.
-        auto period_of = [&](int lo, int nb) {
-            long kb = 1L << 40;
-            for (int j = lo; j < lo + nb; ++j)
-                kb = std::min(kb, static_cast<long>(std::floor(16777216.0 / (pairs_in_bin(j, s) * v2 * v2))));
-            return std::max(1L, kb / (p.f8 ? 64 : 32));  // chunks of 32 bf16 or 64 e4m3 K values
-        };
-        auto total_cost = [&](int G, const int *lo, const int *nb) {
-            double umma[kMaxGroups], all = 0.0;
-            for (int g = 0; g < G; ++g) {
-                umma[g] = 2.0 * blk_cost(lo[g], lo[g] + nb[g] - 1);
-                all += umma[g];
-            }
-            double stall = 0.0;
-            for (int g = 0; g < G; ++g) {
-                const double drain = 0.1 * nb[g] * p.BN * BM;
-                const double cover = 2.0 * (all - umma[g]);
-                stall += std::max(0.0, drain - cover) / static_cast<double>(period_of(lo[g], nb[g]));
-            }
-            return all + stall;
-        };
-        int cur_lo[kMaxGroups], cur_nb[kMaxGroups];
-        for (int g = 0; g < p.G; ++g) {
-            cur_lo[g] = p.blk_lo[g];
-            cur_nb[g] = p.blk_nb[g];
-        }
-        double best_total = total_cost(p.G, cur_lo, cur_nb);
-        auto consider = [&](int G, const int *lo, const int *nb) {
-            const double c = total_cost(G, lo, nb);
-            if (c < best_total - 1e-9) {
-                best_total = c;
-                p.G = G;
-                p.model_cycles_per_kstep = 0.0;
-                for (int g = 0; g < G; ++g) {
-                    p.blk_lo[g] = lo[g];
-                    p.blk_nb[g] = nb[g];
-                    p.model_cycles_per_kstep += blk_cost(lo[g], lo[g] + nb[g] - 1);
-                }
-            }
-        };
-        for (int g = 1; g <= max_groups; ++g) {
-            if (best[g][nbins] >= INF) continue;
-            int lo[kMaxGroups], nb[kMaxGroups];
-            int i = nbins;
-            for (int k = g; k >= 1; --k) {
-                const int f = from[k][i];
-                lo[k - 1] = B0 + f;
-                nb[k - 1] = i - f;
-                i = f;
-            }
-            consider(g, lo, nb);
-        }
-        for (int cut = 1; cut < nbins; ++cut) {
-            if (cut > maxb || nbins - cut > maxb) continue;
-            const int lo[2] = {B0, B0 + cut}, nb[2] = {cut, nbins - cut};
-            consider(2, lo, nb);
-        }
-    }
-    if (hint.groups && hint.sizes[0] > 0) {
+    if (explicit_sizes) {
         // explicit block sizes: contiguous, covering the bins, each at most 256 columns
         int at = B0;
-        double cost = 0.0;
         for (int g = 0; g < hint.groups; ++g) {
             const int nb = hint.sizes[g];
             if (nb < 1 || nb > maxb || at + nb - 1 > B1) {
@@ -380,7 +346,6 @@ bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std
             }
             p.blk_lo[g] = at;
             p.blk_nb[g] = nb;
-            cost += blk_cost(at, at + nb - 1);
             at += nb;
         }
         if (at != B1 + 1) {
@@ -388,7 +353,7 @@ bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std
             return false;
         }
         p.G = hint.groups;
-        p.model_cycles_per_kstep = cost;
+        p.model_cycles_per_kstep = part_cost(p.G, p.blk_lo, p.blk_nb);
     }
     p.pad_lo = 0;
     p.pad_hi = 0;
@@ -459,9 +424,11 @@ bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std
     // ---- drain periods: bin j may accumulate KB_j K-values in fp32 with
     // pairs_j * KB_j * (2^b-1)^2 <= 2^24; a block drains at its tightest bin's
     // period (in chunks).  A period >= n_kc means only after the last chunk.
-    p.min_period = p.n_kc;
+    // Periods and offsets do not depend on K (a period longer than a tile's chunks
+    // only drains at the tile's end), so problems of one shape class share a plan.
+    p.min_period = 1 << 20;
     for (int g = 0; g < p.G; ++g) {
-        int per = p.n_kc;
+        int per = 1 << 20;
         for (int j = p.blk_lo[g]; j < p.blk_lo[g] + p.blk_nb[g]; ++j) {
             const long kbj = static_cast<long>(std::floor(16777216.0 / (pairs_in_bin(j, s) * v2 * v2)));
             per = std::min<long>(per, std::max(1L, kbj / p.KC));
@@ -470,8 +437,7 @@ bool make_plan_uncached(int M, int N, int K, const OzConfig &cfg, Plan *out, std
         p.min_period = std::min(p.min_period, per);
     }
     // stagger the drains of different blocks across chunks
-    for (int g = 0; g < p.G; ++g)
-        p.blk_off[g] = (p.blk_period[g] >= p.n_kc) ? 0 : (g * p.blk_period[g]) / std::max(1, p.G);
+    for (int g = 0; g < p.G; ++g) p.blk_off[g] = (g * p.blk_period[g]) / std::max(1, p.G);
 
     p.tiles_m = (M + BM - 1) / BM;
     p.tiles_n = (N + p.BN - 1) / p.BN;
@@ -637,8 +603,8 @@ double plan_time_model(const Plan &p, int M, int N, int K, int sms) {
     const double units = static_cast<double>(p.tiles_m) * p.tiles_n;
     const double waves = std::ceil(units / std::max(1, sms));
     const int k_per_umma = p.f8 ? 32 : 16;
-    const double umma_per_chunk = static_cast<double>(p.mma_per_kstep) * (p.KC / k_per_umma);
-    const double gemm_s = waves * p.n_kc * umma_per_chunk * 155.0 / 2.0e9;
+    const double ksteps_per_chunk = static_cast<double>(p.KC / k_per_umma);
+    const double gemm_s = waves * p.n_kc * ksteps_per_chunk * p.model_cycles_per_kstep / 2.0e9;
     const double split_bytes = 8.0 * (static_cast<double>(M) * K + static_cast<double>(K) * N) +
                                static_cast<double>(p.a_bytes + p.b_bytes);
     return 1e3 * (gemm_s + split_bytes / 6.5e12);
