@@ -1,12 +1,17 @@
-// Cost of back-to-back tcgen05.mma instructions (cta_group::1) on this GPU, as
-// the planner models it: one CTA per SM, one thread issues `n` UMMAs of a given
-// M, N and kind into R accumulator ranges used round-robin, with operands that
-// change from one instruction to the next; SM cycles per instruction are
-// measured with clock64 between the first issue and the commit's arrival.
+// Cost of back-to-back tcgen05.mma instructions (cta_group::1, M = 128, K = 16,
+// bf16) on this GPU, as the slice-pair GEMM's planner models it.  One CTA per SM;
+// operands change from one instruction to the next; SM cycles per instruction are
+// measured with clock64 from the first issue to the commit's arrival.
 //
-// Prints one line per configuration:  kind M N R cycles_per_umma flop_per_cycle_per_sm
-// Every wait on the commit's mbarrier is bounded (1 s); a timeout prints TIMEOUT
-// and the program exits 3 after releasing TMEM.
+//   tight: one thread issues n UMMAs of width N from a minimal loop (the rate of
+//          the tensor pipe for wide N, the issuing thread's rate for narrow N);
+//   pairs: the 43 UMMAs of one K step of 8 slices with the pair set p + q <= 8,
+//          one per slice pair into its bin's accumulator range, N = 48, dealt
+//          to one or two issuing warps (on different schedulers).
+//
+// Prints one line per case:  mode N issuers cycles_per_umma
+// Every wait on a commit's mbarrier is bounded (1 s); a timeout prints TIMEOUT and
+// the program exits 3 after the kernel has released TMEM.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -19,28 +24,26 @@ using namespace ozgb;
 
 namespace {
 
-constexpr int kASlices = 8;
-constexpr int kABytes = 4096;      // 128 rows x 32 bytes (one K step)
-constexpr int kBBytes = 256 * 32;  // 256 rows x 32 bytes
-constexpr int kBCopies = 4;
-constexpr int kSmem = 120 * 1024;  // more than half of the SM: one CTA per SM (TMEM 512 columns)
+constexpr int kSmem = 160 * 1024;
+constexpr int kTight = 0, kPairs = 1;
 
 struct Cfg {
-    int M, N, R, f8, n_instr;
+    int mode, N, issuers, n_instr;
 };
 
-__global__ void __launch_bounds__(128, 1) umma_cost(const Cfg c, unsigned long long *cycles, int *err) {
+__global__ void __launch_bounds__(128, 1) umma_cost(const Cfg c, unsigned long long *out, int *err) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint8_t *Ab = smem;
-    uint8_t *Bb = smem + kASlices * kABytes;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(Bb + kBCopies * kBBytes);
-    uint32_t *slot = reinterpret_cast<uint32_t *>(bar + 1);
-    for (int i = threadIdx.x * 16; i < kASlices * kABytes + kBCopies * kBBytes; i += blockDim.x * 16)
+    uint8_t *Ab = smem;              // 8 A slices of 128 rows x 32 B
+    uint8_t *Bb = smem + 32 * 1024;  // up to 64 KB of B rows x 32 B
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + 96 * 1024);  // [2]
+    uint32_t *slot = reinterpret_cast<uint32_t *>(bar + 2);
+    for (int i = threadIdx.x * 16; i < 96 * 1024; i += blockDim.x * 16)
         *reinterpret_cast<uint4 *>(smem + i) = make_uint4(0, 0, 0, 0);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     if (threadIdx.x == 0) {
-        mbar_init(bar, 1);
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
         fence_mbar_init();
     }
     const int warp = threadIdx.x >> 5;
@@ -52,36 +55,57 @@ __global__ void __launch_bounds__(128, 1) umma_cost(const Cfg c, unsigned long l
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *slot;
-    if (threadIdx.x == 32) {
+    // issuing threads: lane 0 of warps 1 and 2 (schedulers 1 and 2)
+    const int iss = threadIdx.x == 32 ? 0 : (threadIdx.x == 64 ? 1 : -1);
+    if (iss >= 0 && iss < c.issuers) {
+        const uint32_t id = idesc_bf16_f32(128, c.N);
         const uint64_t a0 = smem_desc(smem_u32(Ab), 128, 256);
         const uint64_t b0 = smem_desc(smem_u32(Bb), 128, 256);
-        const uint32_t id = c.f8 ? idesc_e4m3_f32(c.M, c.N) : idesc_bf16_f32(c.M, c.N);
-        const int dstride = c.R == 1 ? 0 : 512 / c.R;
         const int zero = 0;
         bool ok = true;
-        long long t0 = 0;
+        long long t0 = 0, issued = 0;
         for (int pass = 0; pass < 2 && ok; ++pass) {  // pass 0 warms up
-            if (pass == 1) t0 = clock64();
-            int r = 0, ai = 0, bi = 0;
-            for (int i = 0; i < c.n_instr; ++i) {
-                const uint32_t d = tmem + static_cast<uint32_t>(r * dstride);
-                const uint64_t ad = a0 + static_cast<uint64_t>(ai) * (kABytes >> 4);
-                const uint64_t bd = b0 + static_cast<uint64_t>(bi) * (kBBytes >> 4);
-                const uint32_t acc = (pass == 1 || i >= c.R) ? 1u : 0u;
-                if (c.f8) umma_e4m3(d, ad, bd, id, acc);
-                else umma_bf16(d, ad, bd, id, acc);
-                r = (r + 1 == c.R) ? 0 : r + 1;
-                ai = (ai + 1) & (kASlices - 1);
-                bi = (bi + 1) & (kBCopies - 1);
+            if (pass == 1) {
+                t0 = clock64();
+                issued = 0;
             }
-            umma_commit(bar);
-            ok = mbar_wait(bar, static_cast<uint32_t>(pass), &zero, 1000000000ull);
+            if (c.mode == kTight) {
+                int ai = 0, bi = 0;
+                for (int i = 0; i < c.n_instr; ++i) {
+                    umma_bf16(tmem, a0 + static_cast<uint64_t>(ai) * 256, b0 + static_cast<uint64_t>(bi) * 512, id,
+                              (pass == 1 || i > 0) ? 1u : 0u);
+                    ai = (ai + 1) & 7;
+                    bi = (bi + 1) & 3;
+                }
+                issued = c.n_instr;
+            } else {
+                // bin p + q at TMEM columns (p + q) N; B slice q at q N rows
+                const uint32_t b_step = (c.N * 32) >> 4;
+                const int ksteps = c.n_instr / 43;
+                for (int k = 0; k < ksteps; ++k) {
+                    for (int p = iss; p < 8; p += c.issuers) {
+                        const uint64_t ad = a0 + static_cast<uint64_t>(p) * 256;
+                        const int qmax = 8 - p < 7 ? 8 - p : 7;
+                        uint32_t d = tmem + static_cast<uint32_t>(p * c.N);
+                        uint64_t bd = b0;
+                        for (int q = 0; q <= qmax; ++q) {
+                            umma_bf16(d, ad, bd, id, (pass == 1 || k > 0) ? 1u : 0u);
+                            d += c.N;
+                            bd += b_step;
+                        }
+                        issued += qmax + 1;
+                    }
+                }
+            }
+            umma_commit(&bar[iss]);
+            ok = mbar_wait(&bar[iss], static_cast<uint32_t>(pass), &zero, 1000000000ull);
         }
         const long long t1 = clock64();
-        cycles[blockIdx.x] = ok ? static_cast<unsigned long long>(t1 - t0) : 0ull;
+        out[4 * blockIdx.x + 2 * iss] = ok ? static_cast<unsigned long long>(t1 - t0) : 0ull;
+        out[4 * blockIdx.x + 2 * iss + 1] = static_cast<unsigned long long>(issued);
         if (!ok) {
             atomicExch(err, 1);
-            mbar_wait(bar, 1, &zero, 1000000000ull);  // let issued UMMAs finish before TMEM is freed
+            mbar_wait(&bar[iss], 1, &zero, 1000000000ull);  // let issued UMMAs finish before TMEM is freed
         }
     }
     tc_fence_before();
@@ -103,22 +127,19 @@ int main() {
     int sms = 0;
     check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0), "attribute");
     std::vector<Cfg> cases;
-    // N up to 256; R ranges of 512 / R columns each must hold N
-    for (int N : {16, 48, 96, 128, 192, 240, 256})
-        for (int R : {1, 2, 4})
-            if (R == 1 || N <= 512 / R) cases.push_back({128, N, R, 0, 4096});
-    cases.push_back({64, 256, 1, 0, 4096});
-    cases.push_back({64, 128, 2, 0, 4096});
-    for (int N : {48, 128, 256}) cases.push_back({128, N, 1, 1, 4096});
-    check(cudaFuncSetAttribute(umma_cost, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem + 1024), "attribute");
-    unsigned long long *d_cycles = nullptr;
+    // shared memory: A 32 KB; B 4 copies of up to 8 KB (tight) or 8 slices of N x 32 B (pairs)
+    for (int N : {16, 48, 96, 128, 192, 256}) cases.push_back({kTight, N, 1, 8192});
+    for (int ni : {1, 2}) cases.push_back({kPairs, 48, ni, 43 * 256});
+    check(cudaFuncSetAttribute(umma_cost, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem), "attribute");
+    unsigned long long *d_out = nullptr;
     int *d_err = nullptr;
-    check(cudaMalloc(&d_cycles, sizeof(unsigned long long) * sms), "malloc");
+    check(cudaMalloc(&d_out, sizeof(unsigned long long) * 4 * sms), "malloc");
     check(cudaMalloc(&d_err, sizeof(int)), "malloc");
     check(cudaMemset(d_err, 0, sizeof(int)), "memset");
-    std::vector<unsigned long long> h(sms);
+    std::vector<unsigned long long> h(4 * sms);
     for (const Cfg &c : cases) {
-        umma_cost<<<sms, 128, kSmem + 1024>>>(c, d_cycles, d_err);
+        check(cudaMemset(d_out, 0, sizeof(unsigned long long) * 4 * sms), "memset");
+        umma_cost<<<sms, 128, kSmem>>>(c, d_out, d_err);
         check(cudaGetLastError(), "launch");
         check(cudaDeviceSynchronize(), "kernel");
         int herr = 0;
@@ -127,14 +148,19 @@ int main() {
             std::printf("TIMEOUT\n");
             return 3;
         }
-        check(cudaMemcpy(h.data(), d_cycles, sizeof(unsigned long long) * sms, cudaMemcpyDeviceToHost), "copy");
-        double sum = 0;
-        for (unsigned long long v : h) sum += static_cast<double>(v);
-        const double per = sum / sms / c.n_instr;
-        const double flop = 2.0 * c.M * c.N * (c.f8 ? 32 : 16);
-        std::printf("%s %d %d %d %.1f %.0f\n", c.f8 ? "e4m3" : "bf16", c.M, c.N, c.R, per, flop / per);
+        check(cudaMemcpy(h.data(), d_out, sizeof(unsigned long long) * 4 * sms, cudaMemcpyDeviceToHost), "copy");
+        double cyc = 0, n = 0;
+        for (int i = 0; i < sms; ++i) {
+            double m = 0;
+            for (int j = 0; j < c.issuers; ++j) {
+                m = static_cast<double>(h[4 * i + 2 * j]) > m ? static_cast<double>(h[4 * i + 2 * j]) : m;
+                n += static_cast<double>(h[4 * i + 2 * j + 1]);
+            }
+            cyc += m;
+        }
+        std::printf("%s %d %d %.1f\n", c.mode == kTight ? "tight" : "pairs", c.N, c.issuers, cyc / n);
     }
-    cudaFree(d_cycles);
+    cudaFree(d_out);
     cudaFree(d_err);
     return 0;
 }
