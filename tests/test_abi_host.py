@@ -109,6 +109,25 @@ def test_plan_invariants(ozlib, shape, b, s, J):
     assert max_pairs * c["k_chunk"] * c["drain_chunks"] * (2 ** b - 1) ** 2 <= 2 ** 24
     qmax = sum((_pairs(s, j + 1) - _pairs(s, j)) * K * (2 ** b - 1) ** 2 << (b * (J - 1 - j)) for j in range(J))
     assert qmax.bit_length() + 1 <= 32 * c["acc_words"]
+    # TMEM: one range per bin plus a second range for each double-buffered block
+    dbl = c["dbl_blocks"]
+    assert J * c["tile_n"] + sum(nb[g] * c["tile_n"] for g in range(c["blocks"]) if (dbl >> g) & 1) <= 512
+    assert 1 <= c["issuers"] <= min(3, c["umma_per_kstep"])
+
+
+@pytest.mark.parametrize("s,J,blocks", [(8, 9, [3, 3, 3]), (9, 9, [3, 3, 3]), (9, 10, [4, 3, 3])])
+def test_partition_model_picks_the_measured_best(ozlib, s, J, blocks):
+    """The planner's bin-block cost model picks, at BN = 48, the partition that
+    was fastest among those timed on a GB300 at 4096^3 (sweeps over 6 to 15
+    partitions per schedule), and the plan does not depend on K: its blocks, drain
+    periods and issuers are the same for every K (the problems of a grouped call
+    that share a shape class then share one launch)."""
+    c = ozlib.plan_query(4096, 4096, 4096, 7, s, J)
+    assert c["tile_n"] == 48 and c["block_nb"][:c["blocks"]] == blocks and c["issuers"] == 3
+    for K in (32, 300, 4096, 65536):
+        d = ozlib.plan_query(4096, 4096, K, 7, s, J)
+        for key in ("tile_n", "blocks", "block_lo", "block_nb", "issuers", "dbl_blocks", "drain_chunks"):
+            assert d[key] == c[key], (K, key)
 
 
 def test_plan_rejects_inexact_requests(ozlib):
