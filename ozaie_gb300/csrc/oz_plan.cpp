@@ -625,6 +625,8 @@ Schedule choose_schedule(const KnobStats &k, int M, int N, int K, const OzConfig
     for (int s = s_min; s <= s_max; ++s) {
         if (first_ok && s > first_ok + 3) break;  // a product with 4 more slices is not cheaper
         const int j_max = any_set ? std::min(2 * s - 1, 32) : s;
+        // the estimate does not grow with J: no J meets the bound if the largest does not
+        if (!(knob_estimate_set(k, K, base.b, s, std::max(s, j_max), crit, tail) <= bound)) continue;
         for (int J = s; J <= std::max(s, j_max); ++J) {
             const double est = knob_estimate_set(k, K, base.b, s, J, crit, tail);
             if (!(est <= bound)) continue;
