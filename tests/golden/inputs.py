@@ -56,7 +56,7 @@ def uniform64(seed, lo, hi, count):
     return vals
 
 
-def config1_inputs():
+def uniform_256x512x128_inputs():
     """Row-major A (256 x 128) and B (128 x 512), uniform(-1, 1), one
     mt19937_64(0) stream drawn A first, then B."""
     M, N, K = 256, 512, 128

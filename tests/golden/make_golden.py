@@ -11,11 +11,11 @@ Fixtures:
   harness.npz      small A, B drawn by the Oz-AIE test-harness formula
                    (test.cpp:219-237, phi in {0.5, 1, 2, 4}) with the exact and the
                    MPFR-106 value of every entry of A B: pins the final results.
-  config1.json     the 256 x 512 x 128 uniform(-1, 1) mt19937_64(0) workload: input
+  uniform_256x512x128.json     the 256 x 512 x 128 uniform(-1, 1) mt19937_64(0) workload: input
                    digests from the C++ standard library, and digests of every
                    intermediate of the oracle in both profiles, so that the device
                    path can be compared against them without running the oracle.
-  config1_small.npz  the exponents and 64 sampled MPFR-106 values of that workload.
+  uniform_256x512x128_mpfr.npz  the exponents and 64 sampled MPFR-106 values of that workload.
 """
 import json
 import os
@@ -99,12 +99,12 @@ def make_harness(tmp):
     np.savez_compressed(os.path.join(HERE, "harness.npz"), **out)
 
 
-def make_config1(tmp):
+def make_uniform_256x512x128(tmp):
     M, N, K = 256, 512, 128
     v = _gen(tmp, "uniform64", 0, -1.0, 1.0, M * K + K * N)
     A = v[:M * K].reshape(M, K)
     B = v[M * K:].reshape(K, N)
-    pa, pb = inputs.config1_inputs()
+    pa, pb = inputs.uniform_256x512x128_inputs()
     if not (np.array_equal(pa, A) and np.array_equal(pb, B)):
         raise SystemExit("the Python mt19937_64 restatement differs from the C++ standard library")
     H = inputs.sha256
@@ -137,8 +137,8 @@ def make_config1(tmp):
     mp = O.mpfr_entries(A, B, r, c)
     if mp is None:
         raise SystemExit("libmpfr.so.6 not found")
-    np.savez_compressed(os.path.join(HERE, "config1_small.npz"), er=er, ec=ec, rows=r, cols=c, mpfr=mp)
-    with open(os.path.join(HERE, "config1.json"), "w") as f:
+    np.savez_compressed(os.path.join(HERE, "uniform_256x512x128_mpfr.npz"), er=er, ec=ec, rows=r, cols=c, mpfr=mp)
+    with open(os.path.join(HERE, "uniform_256x512x128.json"), "w") as f:
         json.dump(doc, f, indent=1)
         f.write("\n")
 
@@ -148,7 +148,7 @@ def main():
     with tempfile.TemporaryDirectory() as tmp:
         make_decode(rng)
         make_harness(tmp)
-        make_config1(tmp)
+        make_uniform_256x512x128(tmp)
     print("fixtures written to", HERE)
 
 

@@ -30,16 +30,16 @@ def _dgemm(h, A, B, mode):
 
 
 @pytest.fixture(scope="module")
-def config1():
-    doc = json.load(open(os.path.join(GOLDEN, "config1.json")))
-    A, B = inputs.config1_inputs()
+def uniform_256x512x128():
+    doc = json.load(open(os.path.join(GOLDEN, "uniform_256x512x128.json")))
+    A, B = inputs.uniform_256x512x128_inputs()
     assert H(A) == doc["A"] and H(B) == doc["B"]
     return doc, np.ascontiguousarray(A), np.ascontiguousarray(B)
 
 
 @pytest.mark.parametrize("s", [8, 9])
-def test_config1_north_star_profile(gpu_handle, config1, s):
-    doc, A, B = config1
+def test_uniform_256x512x128_gb300_profile(gpu_handle, uniform_256x512x128, s):
+    doc, A, B = uniform_256x512x128
     want = doc["profiles"]["b7_s%d_tri_rn" % s]
     gpu_handle.set_slices(s)
     gpu_handle.set_bins(s)
@@ -51,11 +51,11 @@ def test_config1_north_star_profile(gpu_handle, config1, s):
 
 
 @pytest.mark.parametrize("name,mode", [("ref_accurate_b3_d29", 0), ("ref_fast_b7_d8", 1)])
-def test_config1_reference_profile(gpu_handle, config1, name, mode):
+def test_uniform_256x512x128_reference_profile(gpu_handle, uniform_256x512x128, name, mode):
     """The reference's own tables and truncating decode: the slices and the final
     bits equal those of the reference's arithmetic (its compiled decode made the
     fixture)."""
-    doc, A, B = config1
+    doc, A, B = uniform_256x512x128
     want = doc["profiles"][name]
     gpu_handle.set_profile(1)
     C = _dgemm(gpu_handle, A, B, mode)
@@ -64,9 +64,9 @@ def test_config1_reference_profile(gpu_handle, config1, name, mode):
     assert H(d["a_slices"]) == want["a_slices"] and H(d["b_slices"]) == want["b_slices"]
 
 
-def test_config1_against_mpfr(gpu_handle, config1):
-    _, A, B = config1
-    z = np.load(os.path.join(GOLDEN, "config1_small.npz"))
+def test_uniform_256x512x128_against_mpfr(gpu_handle, uniform_256x512x128):
+    _, A, B = uniform_256x512x128
+    z = np.load(os.path.join(GOLDEN, "uniform_256x512x128_mpfr.npz"))
     gpu_handle.set_error_bound(1e-15)
     C = _dgemm(gpu_handle, A, B, 1)[z["rows"], z["cols"]]
     mp = z["mpfr"]

@@ -238,20 +238,20 @@ def test_exact_entries_are_correctly_rounded(oracle):
 
 
 # ------------------------------------------------------------ golden fixtures
-def test_config1_generator_matches_cpp_fixture():
+def test_uniform_256x512x128_generator_matches_cpp_fixture():
     from golden import inputs
-    doc = json.load(open(os.path.join(GOLDEN, "config1.json")))
-    A, B = inputs.config1_inputs()
+    doc = json.load(open(os.path.join(GOLDEN, "uniform_256x512x128.json")))
+    A, B = inputs.uniform_256x512x128_inputs()
     assert inputs.sha256(A) == doc["A"] and inputs.sha256(B) == doc["B"]
 
 
-def test_config1_oracle_intermediates(oracle):
+def test_uniform_256x512x128_oracle_intermediates(oracle):
     """Every oracle intermediate of the 256 x 512 x 128 workload against the
     committed digests (made where the reference's decode was compiled)."""
     from golden import inputs
     H = inputs.sha256
-    doc = json.load(open(os.path.join(GOLDEN, "config1.json")))
-    A, B = inputs.config1_inputs()
+    doc = json.load(open(os.path.join(GOLDEN, "uniform_256x512x128.json")))
+    A, B = inputs.uniform_256x512x128_inputs()
     M, N, K = doc["shape"]
     er, ec = oracle.max_exp_rows(A), oracle.max_exp_cols(B)
     assert H(er) == doc["er"] and H(ec) == doc["ec"]
@@ -271,12 +271,12 @@ def test_config1_oracle_intermediates(oracle):
             [want[k] for k in ("a_slices", "b_slices", "bins", "pairs", "C")]
 
 
-def test_config1_results_against_mpfr(oracle):
+def test_uniform_256x512x128_results_against_mpfr(oracle):
     """The reference's correctness gate (common.h:338-341: relative 0.05 or absolute
     0.5 against MPFR-106) and the tighter bound of this library."""
     from golden import inputs
-    z = np.load(os.path.join(GOLDEN, "config1_small.npz"))
-    A, B = inputs.config1_inputs()
+    z = np.load(os.path.join(GOLDEN, "uniform_256x512x128_mpfr.npz"))
+    A, B = inputs.uniform_256x512x128_inputs()
     r, c, mp = z["rows"], z["cols"], z["mpfr"]
     ref_acc = oracle.dgemm(A, B, 3, 29, 29, 1)[r, c]
     assert np.all((np.abs(ref_acc - mp) <= 0.5) | (np.abs(ref_acc - mp) <= 0.05 * np.abs(mp)))
