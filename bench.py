@@ -343,6 +343,48 @@ def sampled_errors(dA, dB, dC, n, seed, O, torch, tail=1e-4, mpfr=True):
     return out
 
 
+def cublas_emulated_run(dA, dB, dC, A, B, r, c, exact, absdot, O, torch):
+    """cuBLAS's own fixed-point FP64 emulation on the headline workload, for
+    comparison, with the eager strategy: through cublasGemmEx's compute type
+    CUBLAS_COMPUTE_64F_EMULATED_FIXEDPOINT, and through cublasDgemm under the math
+    mode CUBLAS_FP64_EMULATED_FIXEDPOINT_MATH (mantissa bits chosen by cuBLAS at run
+    time, and fixed at 53).  tests/perf/cublas_dgemm.cu is compiled here when nvcc is
+    present; any failure is reported, not raised."""
+    import ctypes
+    import shutil
+    import subprocess
+    import tempfile
+    try:
+        nvcc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+        nvcc = nvcc if os.path.exists(nvcc) else shutil.which("nvcc")
+        if not nvcc:
+            return {"unavailable": "nvcc not found"}
+        so = os.path.join(tempfile.mkdtemp(prefix="oz_cublas_"), "libcublas_dgemm.so")
+        subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-std=c++17", "-Xcompiler", "-fPIC",
+                        "-shared", "-o", so, os.path.join(ROOT, "tests", "perf", "cublas_dgemm.cu"), "-lcublas"],
+                       check=True, capture_output=True, timeout=300)
+        L = ctypes.CDLL(so)
+        L.cublas_dgemm_timed.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p] * 3 + [ctypes.c_int] * 3 + \
+            [ctypes.POINTER(ctypes.c_float)]
+        M, K = dA.shape
+        N = dB.shape[1]
+        out = {}
+        for name, mode, bits in (("gemmex_compute_type", 1, 0), ("math_mode", 2, 0), ("math_mode_53_bits", 2, 53)):
+            ms = ctypes.c_float(0.0)
+            torch.cuda.synchronize()
+            rc = L.cublas_dgemm_timed(M, N, K, dA.data_ptr(), dB.data_ptr(), dC.data_ptr(), mode, bits, 5,
+                                      ctypes.byref(ms))
+            torch.cuda.synchronize()
+            if rc:
+                out[name] = {"unavailable": "cublas_dgemm_timed returned %d" % rc}
+                continue
+            out[name] = {"value": 2.0 * M * N * K / (ms.value * 1e-3) / 1e12, "unit": UNIT, "ms": ms.value,
+                         "accuracy_vs_exact": O.error_report(dC.cpu().numpy(), A, B, r, c, exact, absdot)}
+        return out
+    except Exception as e:  # the comparison line must not stop the benchmark
+        return {"unavailable": "%s: %s" % (type(e).__name__, str(e)[:200])}
+
+
 def time_device(fn, torch, stream, reps=1):
     """Mean device time (ms) of fn() over reps calls, CUDA events on the stream."""
     e0 = torch.cuda.Event(enable_timing=True)
@@ -886,6 +928,7 @@ def main():
     torch.cuda.synchronize()
     cublas_ms = c0.elapsed_time(c1) / 3
     err_cublas = O.error_report(dC.cpu().numpy(), A, B, r, c, exact, absdot)
+    cublas_emulated = cublas_emulated_run(dA, dB, dC, A, B, r, c, exact, absdot, O, torch) if rank == 0 else None
 
     batched = batched_run(args.batched, dev, stream, oz, O, torch) if args.batched > 0 and rank == 0 else None
     long_k = long_k_run(dev, stream, oz, O, torch) if not args.no_longk and rank == 0 else None
@@ -922,6 +965,7 @@ def main():
             "elementwise_mode": elementwise_mode,
             "stage_ms": {k: statistics.median([t[k] for t in stage]) for k in stage[0]},
             "cublas_dgemm": {"value": flops / (cublas_ms * 1e-3) / 1e12, "unit": UNIT, "ms": cublas_ms},
+            "cublas_fp64_emulated": cublas_emulated,
             "e2e": {"value": flops / (e2e_ms * 1e-3) / 1e12, "unit": UNIT, "ms_per_step": e2e_ms,
                     "host_memory": "pageable (plain numpy arrays)",
                     "h2d_bytes_per_step": 2 * M * K * 8, "d2h_bytes_per_step": M * N * 8,
