@@ -8,8 +8,8 @@
 //   int128 -> double reconstruction                include/oz_aie.h:92-150
 //
 // GB300 design (persistent CTAs, one per SM, each looping over 128 x BN tiles of
-// C; 608 threads: producer warp, MMA-issuer warp, 16 drain/epilogue warps, and a
-// second MMA-issuer warp that takes half of the bin blocks when the plan says so):
+// C; 640 threads: a producer warp, 16 drain/epilogue warps and up to three
+// MMA-issuing warps on three schedulers):
 //   * Carrier: tcgen05.mma kind::f16 with bf16 slices (|v| <= 127 is exact in
 //     bf16) and fp32 accumulators in TMEM.  (kind::i8 is not accepted by ptxas
 //     for sm_103a.)  Slices of b <= 4 bits may instead be e4m3 (kind::f8f6f4,
@@ -18,28 +18,30 @@
 //     partial sum is an integer of magnitude <= 2^24 as
 //     long as bin j accumulates at most KB_j K-values between drains,
 //     pairs_in_bin(j) * KB_j * (2^b-1)^2 <= 2^24, so the fp32 accumulation is exact.
-//   * TMEM holds one fp32 accumulator of BN columns per bin j (column j*BN).
+//   * TMEM holds one fp32 accumulator of BN columns per bin j (column j*BN), and
+//     a second range for each double-buffered block where the columns allow it.
 //     Bins are partitioned into up to 8 blocks of at most 256 columns.  Every
 //     UMMA of a block spans the whole block: A slice p against the B slices
 //     q = j - p of all bins j of the block, which are consecutive in shared
 //     memory; q outside [0, s) reads zero slices padded below and above the
-//     loaded ones.  On GB300 one M=128, K=16 UMMA costs max(~114, N/2) cycles
-//     and a UMMA into an accumulator range that partly overlaps the previous
-//     one costs more, so full-block UMMAs (large N, identical ranges) beat
-//     per-pair ones despite the padded zero work.  The planner picks the
-//     partition with a dynamic program over that cost.
+//     loaded ones.  On GB300 one M=128, K=16 UMMA occupies the tensor pipe for
+//     N/2 cycles, and one issuing thread issues one about every 80-100 cycles,
+//     so wide UMMAs from several issuers feed the pipe; the planner picks the
+//     partition with a cost model fitted to this kernel.
+//   * The UMMA runs of a K step (block, A slice) are dealt round-robin to the
+//     issuing warps, which all accumulate (enable_input_d = 1): the drain warps
+//     store zeros over every accumulator they read out, and TMEM starts zeroed.
 //   * Each block is a drain group with its own period (its tightest bin).  In
-//     each chunk the MMA issuer first issues the blocks that drain after this
-//     chunk, then the others, and last the blocks drained after the previous
-//     chunk (after waiting for their drain): a drain overlaps the UMMAs of the
-//     other blocks.  The first UMMA of a block after a drain overwrites the
-//     accumulators (enable_input_d = 0), so TMEM is never cleared explicitly.
+//     each chunk the issuers first issue the blocks that drain after this chunk,
+//     then the others, and last the blocks drained after the previous chunk
+//     (after waiting for their drain): a drain overlaps the UMMAs of the other
+//     blocks.  A double-buffered block switches ranges at each drain instead.
 //   * Drain (warps 2..17): TMEM -> registers, fp32 -> int32 (exact), then one
 //     32 x 32 -> 64-bit multiply-add by 2^rel into the 64-bit accumulator of the
 //     bin's group (consecutive bins whose weights relative to the group's first
 //     bin stay <= 2^30).  The W-word exact sum is assembled once per element in
-//     the epilogue.  Integer ALU work competes with the MMA-issuing thread on its
-//     scheduler, so the drain keeps it to two instructions per value.
+//     the epilogue.  Integer ALU work competes with the MMA-issuing warps on their
+//     schedulers, so the drain keeps it to two instructions per value.
 //   * The last partial wave of a launch may be split along K (split_parts): the
 //     parts add their 64-bit group sums into global scratch with atomics and
 //     the part that completes a tile's count rounds and stores it.
