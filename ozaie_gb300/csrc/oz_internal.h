@@ -124,7 +124,7 @@ struct GemmArgs {
     // below 2^63.  OUT_PAIRS: groups {0, pair_g0}, each modulo 2^64.
     int n_acc;
     int acc_t0[kMaxAcc];
-    int n_iss;  // MMA-issuing threads: 2 splits the bin blocks by index parity (G >= 2)
+    int n_iss;  // MMA-issuing warps (1 to 3): the UMMA runs of a K step are dealt round-robin
     double alpha, beta;  // C = alpha * (A B) + beta * C for OUT_RN / OUT_RZ_REF (1, 0: plain store)
 };
 

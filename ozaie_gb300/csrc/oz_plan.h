@@ -34,7 +34,7 @@ struct Plan {
     int blk_lo[kMaxGroups] = {0}, blk_nb[kMaxGroups] = {0}, blk_p0[kMaxGroups] = {0}, blk_p1[kMaxGroups] = {0};
     int blk_period[kMaxGroups] = {0}, blk_off[kMaxGroups] = {0};
     int n_acc = 0, acc_t0[kMaxAcc] = {0};  // drain accumulator groups (GemmArgs)
-    int n_iss = 1;                         // MMA-issuing threads
+    int n_iss = 1;                         // MMA-issuing warps (1 to 3)
     uint32_t dbl_mask = 0;                 // double-buffered blocks (GemmArgs)
     int blk_col1[kMaxGroups] = {0};        // their second accumulator range (TMEM column)
     GemmLaunchFn fn = nullptr;
@@ -55,7 +55,7 @@ struct PlanHints {
     int BN = 0, KC = 0, groups = 0, stages = 0;
     int sizes[kMaxGroups] = {0};  // explicit bin-block sizes (groups of them), overriding the cost model
     int min_W = 0;                // at least this many accumulator words (4 for OUT_PAIRS)
-    int issuers = 0;              // MMA-issuing threads (1 or 2)
+    int issuers = 0;              // MMA-issuing warps (1 to 3)
     int dbl = -1;                 // double-buffered blocks: -1 the planner's choice, 0 none, 1 every one that fits
 };
 
@@ -148,9 +148,9 @@ struct Schedule {
 };
 
 // Modelled time (ms) of one M x N x K product with a plan on `sms` SMs: the
-// slice-pair GEMM's UMMA count at 155 SM cycles each (measured on GB300 for
-// every N <= 256 and both carriers) at 2 GHz, over whole waves of tiles, plus the
-// HBM traffic of the split at 6.5 TB/s.
+// plan's modelled SM cycles per K step (model_cycles_per_kstep, the bin-block cost
+// model fitted to the slice-pair GEMM on GB300) at 2 GHz, over whole waves of
+// tiles, plus the HBM traffic of the split at 6.5 TB/s.
 double plan_time_model(const Plan &p, int M, int N, int K, int sms);
 
 // The slice schedule for a requested bound: among s in [s_min, s_max] and, with
