@@ -359,11 +359,12 @@ def cublas_emulated_run(dA, dB, dC, A, B, r, c, exact, absdot, O, torch):
         nvcc = nvcc if os.path.exists(nvcc) else shutil.which("nvcc")
         if not nvcc:
             return {"unavailable": "nvcc not found"}
-        so = os.path.join(tempfile.mkdtemp(prefix="oz_cublas_"), "libcublas_dgemm.so")
-        subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-std=c++17", "-Xcompiler", "-fPIC",
-                        "-shared", "-o", so, os.path.join(ROOT, "tests", "perf", "cublas_dgemm.cu"), "-lcublas"],
-                       check=True, capture_output=True, timeout=300)
-        L = ctypes.CDLL(so)
+        with tempfile.TemporaryDirectory(prefix="oz_cublas_") as tmp:
+            so = os.path.join(tmp, "libcublas_dgemm.so")
+            subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-std=c++17", "-Xcompiler",
+                            "-fPIC", "-shared", "-o", so, os.path.join(ROOT, "tests", "perf", "cublas_dgemm.cu"),
+                            "-lcublas"], check=True, capture_output=True, timeout=300)
+            L = ctypes.CDLL(so)  # stays mapped after the directory is removed
         L.cublas_dgemm_timed.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p] * 3 + [ctypes.c_int] * 3 + \
             [ctypes.POINTER(ctypes.c_float)]
         M, K = dA.shape
